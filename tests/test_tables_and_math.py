@@ -1,0 +1,75 @@
+"""Tag family tables (reference test_family_tables, test_detector.cpp:70-102)
+and the accuracy of the deterministic math helpers (detmath.h)."""
+import re
+from pathlib import Path
+
+import numpy as np
+
+import oracle
+
+INC = Path(__file__).resolve().parent.parent / "bd-cudatag_gb300" / "csrc" / "families_data.inc"
+
+
+def load_tables():
+    text = INC.read_text()
+    out = {}
+    for name in ("kCodewords36h11", "kCodewords16h5"):
+        body = re.search(name + r"\[(\d+)\] = \{(.*?)\};", text, re.S)
+        vals = [int(v, 16) for v in re.findall(r"0x([0-9a-f]+)ull", body.group(2))]
+        assert len(vals) == int(body.group(1))
+        out[name] = vals
+    return out["kCodewords36h11"], out["kCodewords16h5"]
+
+
+def rotate(codes: np.ndarray, bits: int) -> np.ndarray:
+    n = bits * bits
+    out = np.zeros_like(codes)
+    for r in range(bits):
+        for c in range(bits):
+            bit = (codes >> np.uint64(n - 1 - (r * bits + c))) & np.uint64(1)
+            out |= bit << np.uint64(n - 1 - (c * bits + (bits - 1 - r)))
+    return out
+
+
+def popcount(x: np.ndarray) -> np.ndarray:
+    return np.unpackbits(x.view(np.uint8).reshape(*x.shape, 8), axis=-1).sum(-1)
+
+
+def min_distance(codes, bits):
+    a = np.array(codes, dtype=np.uint64)
+    best = 1000
+    rot = a.copy()
+    for k in range(4):
+        d = popcount(a[:, None] ^ rot[None, :])
+        if k == 0:
+            np.fill_diagonal(d, 1000)
+        best = min(best, int(d.min()))
+        rot = rotate(rot, bits)
+    return best
+
+
+def test_family_tables():
+    t36, t16 = load_tables()
+    assert len(t36) == 587 and len(t16) == 30
+    assert max(t36) < 1 << 36 and max(t16) < 1 << 16
+    assert min_distance(t36, 6) == 11
+    assert min_distance(t16, 4) == 5
+
+
+def test_detmath_accuracy():
+    L = oracle.lib()
+    rng = np.random.default_rng(1)
+    xs = np.concatenate([rng.uniform(-7.0, 7.0, 4000), np.linspace(-3.2, 3.2, 257)]).astype(np.float32)
+    for x in xs:
+        s, c = L.bdo_sinf(float(x)), L.bdo_cosf(float(x))
+        assert abs(s - np.sin(np.float64(x))) <= 3e-7
+        assert abs(c - np.cos(np.float64(x))) <= 3e-7
+    ys = rng.uniform(-50, 50, (3000, 2)).astype(np.float32)
+    for y, x in ys:
+        a = L.bdo_atan2f(float(y), float(x))
+        ref = np.arctan2(np.float64(y), np.float64(x))
+        assert abs(a - ref) <= 4e-7 * max(1.0, abs(ref))
+    # signed zeros as C99 Annex F
+    assert L.bdo_atan2f(0.0, -0.0) == np.float32(np.pi)
+    assert L.bdo_atan2f(-0.0, -0.0) == -np.float32(np.pi)
+    assert np.signbit(L.bdo_atan2f(-0.0, 0.0))
