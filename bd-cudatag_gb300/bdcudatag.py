@@ -1,0 +1,308 @@
+"""ctypes binding of libbdcudatag.so (the GB300 detector library).
+
+The structure mirrors and the function signatures are those of the
+reference's own ctypes consumer (detector/bench/compare_detectors.py:76-156),
+so code written against the reference binds this library unchanged; the
+batch entry points of bdcudatag_gb300.h are added.
+
+Loading fails loudly when the library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libbdcudatag.so"
+
+FAMILY_TAG36H11 = 0
+FAMILY_TAG16H5 = 1
+OK = 0
+ERROR_INVALID_ARGUMENT = -1
+ERROR_CUDA = -2
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("max_hamming", ctypes.c_int32),
+        ("min_cluster_pixels", ctypes.c_int32),
+        ("min_tag_pixels", ctypes.c_int32),
+        ("max_detections", ctypes.c_int32),
+        ("max_candidates", ctypes.c_int32),
+        ("refine_edges", ctypes.c_int32),
+        ("use_cuda_graph", ctypes.c_int32),
+        ("min_decision_margin", ctypes.c_float),
+        ("decode_sharpening", ctypes.c_float),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("frames", ctypes.c_uint64),
+        ("last_gpu_ms", ctypes.c_float),
+        ("average_gpu_ms", ctypes.c_float),
+        ("last_total_ms", ctypes.c_float),
+        ("runs", ctypes.c_int32),
+        ("candidates", ctypes.c_int32),
+        ("detections", ctypes.c_int32),
+        ("quads", ctypes.c_int32),
+        ("roi_rows", ctypes.c_int32),
+    ]
+
+
+class Detection(ctypes.Structure):
+    _fields_ = [
+        ("id", ctypes.c_int32),
+        ("hamming", ctypes.c_int32),
+        ("decision_margin", ctypes.c_float),
+        ("corners", ctypes.c_float * 8),
+        ("reserved", ctypes.c_int32),
+        ("homography", ctypes.c_float * 9),
+    ]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("families", ctypes.c_uint32), ("reserved", ctypes.c_int32)]
+
+
+DETECTION_DTYPE = np.dtype([("id", "<i4"), ("hamming", "<i4"), ("decision_margin", "<f4"),
+                            ("corners", "<f4", (8,)), ("reserved", "<i4"),
+                            ("homography", "<f4", (9,))])
+assert DETECTION_DTYPE.itemsize == ctypes.sizeof(Detection) == 84
+assert ctypes.sizeof(Config) == 40 and ctypes.sizeof(Stats) == 40 and ctypes.sizeof(Camera) == 16
+
+# Every C symbol the library exports (include/bdcudatag/*.h).
+REFERENCE_SYMBOLS = [
+    "bd_api_version", "bd_version_string", "bd_family_count", "bd_family_name",
+    "bd_family_bits_per_side", "bd_family_min_hamming", "bd_family_default_max_hamming",
+    "bd_config_init", "bd_detector_create", "bd_detector_destroy", "bd_detector_detect_host",
+    "bd_detector_detect_device", "bd_detector_get_stats", "bd_last_error",
+]
+GB300_SYMBOLS = [
+    "bd_batch_create", "bd_batch_destroy", "bd_batch_camera_count", "bd_batch_max_detections",
+    "bd_batch_device_bytes", "bd_batch_detect_host", "bd_batch_detect_device",
+    "bd_batch_submit_host", "bd_batch_submit_device", "bd_batch_wait", "bd_batch_host_frame",
+    "bd_batch_last_gpu_ms", "bd_batch_counts", "bd_batch_debug_stage", "bd_detector_debug_stage",
+]
+
+_LIB = None
+_P = ctypes.c_void_p
+
+
+def lib() -> ctypes.CDLL:
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
+        L = ctypes.CDLL(str(LIB_PATH))
+        L.bd_api_version.restype = ctypes.c_uint32
+        L.bd_version_string.restype = ctypes.c_char_p
+        L.bd_family_name.restype = ctypes.c_char_p
+        L.bd_family_name.argtypes = [ctypes.c_int32]
+        for n in ("bd_family_bits_per_side", "bd_family_min_hamming", "bd_family_default_max_hamming"):
+            getattr(L, n).argtypes = [ctypes.c_int32]
+            getattr(L, n).restype = ctypes.c_int32
+        L.bd_config_init.argtypes = [ctypes.POINTER(Config)]
+        L.bd_detector_create.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_int32)]
+        L.bd_detector_create.restype = _P
+        L.bd_detector_destroy.argtypes = [_P]
+        for n in ("bd_detector_detect_host", "bd_detector_detect_device"):
+            getattr(L, n).argtypes = [_P, _P, ctypes.c_int32, _P, ctypes.c_int32]
+            getattr(L, n).restype = ctypes.c_int32
+        L.bd_detector_get_stats.argtypes = [_P, ctypes.POINTER(Stats)]
+        L.bd_last_error.restype = ctypes.c_char_p
+        L.bd_batch_create.argtypes = [_P, ctypes.c_int32, ctypes.POINTER(Config),
+                                      ctypes.POINTER(ctypes.c_int32)]
+        L.bd_batch_create.restype = _P
+        L.bd_batch_destroy.argtypes = [_P]
+        L.bd_batch_camera_count.argtypes = [_P]
+        L.bd_batch_max_detections.argtypes = [_P]
+        L.bd_batch_device_bytes.argtypes = [_P]
+        L.bd_batch_device_bytes.restype = ctypes.c_int64
+        for n in ("bd_batch_detect_host", "bd_batch_detect_device"):
+            getattr(L, n).argtypes = [_P, _P, _P, _P, _P]
+            getattr(L, n).restype = ctypes.c_int32
+        for n in ("bd_batch_submit_host", "bd_batch_submit_device"):
+            getattr(L, n).argtypes = [_P, _P, _P]
+            getattr(L, n).restype = ctypes.c_int32
+        L.bd_batch_wait.argtypes = [_P, _P, _P]
+        L.bd_batch_wait.restype = ctypes.c_int32
+        L.bd_batch_host_frame.argtypes = [_P, ctypes.c_int32]
+        L.bd_batch_host_frame.restype = _P
+        L.bd_batch_last_gpu_ms.argtypes = [_P]
+        L.bd_batch_last_gpu_ms.restype = ctypes.c_float
+        L.bd_batch_counts.argtypes = [_P, ctypes.c_int32, _P]
+        L.bd_batch_debug_stage.argtypes = [_P, ctypes.c_int32, ctypes.c_char_p, _P, ctypes.c_int64]
+        L.bd_batch_debug_stage.restype = ctypes.c_int64
+        L.bd_detector_debug_stage.argtypes = [_P, ctypes.c_char_p, _P, ctypes.c_int64]
+        L.bd_detector_debug_stage.restype = ctypes.c_int64
+        _LIB = L
+    return _LIB
+
+
+def default_config(**overrides) -> Config:
+    c = Config()
+    lib().bd_config_init(ctypes.byref(c))
+    for k, v in overrides.items():
+        setattr(c, k, v)
+    return c
+
+
+def last_error() -> str:
+    msg = lib().bd_last_error()
+    return msg.decode() if msg else ""
+
+
+def _ptr(x) -> int:
+    """Address of a numpy array, a torch tensor (host or device) or an int."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+_STAGE_DTYPES = {
+    "tile_min": np.uint8, "tile_max": np.uint8, "bits": np.uint32, "row_count": np.uint32,
+    "runs": np.uint32, "label": np.uint32, "area": np.uint32, "bbox": np.uint32,
+    "candidates": np.uint32, "hull_quads": np.float32, "quads": np.float32,
+    "decodes": np.dtype([("id", "<i4"), ("hamming", "<i4"), ("margin", "<f4"), ("corners", "<f4", (8,))]),
+    "state": np.uint32,
+}
+
+
+def _stage(fn, *args, name: str) -> np.ndarray:
+    size = fn(*args, name.encode(), None, 0)
+    if size < 0:
+        raise KeyError(name)
+    dt = np.dtype(_STAGE_DTYPES[name])
+    out = np.zeros(size // dt.itemsize, dtype=dt)
+    fn(*args, name.encode(), out.ctypes.data, size)
+    return out
+
+
+class Detector:
+    """One family, one frame size: the reference's bd_detector."""
+
+    def __init__(self, family: int, width: int, height: int, config: Config | None = None):
+        status = ctypes.c_int32(0)
+        cfg = config if config is not None else default_config()
+        self.handle = lib().bd_detector_create(family, width, height, ctypes.byref(cfg),
+                                               ctypes.byref(status))
+        if not self.handle:
+            raise RuntimeError(f"bd_detector_create failed ({status.value}): {last_error()}")
+        self.family, self.width, self.height = family, width, height
+        self.max_detections = min(max(cfg.max_detections, 1), 256)
+        self.out = np.zeros(self.max_detections, dtype=DETECTION_DTYPE)
+
+    def detect(self, gray: np.ndarray, stride: int | None = None, capacity: int | None = None):
+        """Returns (found, detections written)."""
+        cap = self.max_detections if capacity is None else capacity
+        s = gray.strides[0] if stride is None else stride
+        n = lib().bd_detector_detect_host(self.handle, _ptr(gray), s, self.out.ctypes.data, cap)
+        if n < 0:
+            raise RuntimeError(f"detect failed ({n}): {last_error()}")
+        return n, self.out[:min(n, cap)].copy()
+
+    def detect_device(self, gray_device, stride: int, capacity: int | None = None):
+        cap = self.max_detections if capacity is None else capacity
+        n = lib().bd_detector_detect_device(self.handle, _ptr(gray_device), stride,
+                                            self.out.ctypes.data, cap)
+        if n < 0:
+            raise RuntimeError(f"detect_device failed ({n}): {last_error()}")
+        return n, self.out[:min(n, cap)].copy()
+
+    def stats(self) -> Stats:
+        s = Stats()
+        lib().bd_detector_get_stats(self.handle, ctypes.byref(s))
+        return s
+
+    def stage(self, name: str) -> np.ndarray:
+        return _stage(lib().bd_detector_debug_stage, self.handle, name=name)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().bd_detector_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+
+class Batch:
+    """A fixed set of cameras detected together (bd_batch)."""
+
+    def __init__(self, cameras: list[tuple[int, int, int]], config: Config | None = None):
+        arr = (Camera * len(cameras))(*[Camera(w, h, fam, 0) for w, h, fam in cameras])
+        status = ctypes.c_int32(0)
+        cfg = config if config is not None else default_config()
+        self.handle = lib().bd_batch_create(ctypes.cast(arr, _P), len(cameras), ctypes.byref(cfg),
+                                            ctypes.byref(status))
+        if not self.handle:
+            raise RuntimeError(f"bd_batch_create failed ({status.value}): {last_error()}")
+        self.cameras = list(cameras)
+        self.n = len(cameras)
+        self.max_detections = lib().bd_batch_max_detections(self.handle)
+        self.out = np.zeros((self.n, 2, self.max_detections), dtype=DETECTION_DTYPE)
+        self.found = np.zeros((self.n, 2), dtype=np.int32)
+        self._ptrs = (ctypes.c_void_p * self.n)()
+        self._strides = np.zeros(self.n, dtype=np.int32)
+
+    def _set(self, frames, strides):
+        for i, f in enumerate(frames):
+            self._ptrs[i] = _ptr(f)
+            self._strides[i] = strides[i] if strides is not None else \
+                (f.strides[0] if hasattr(f, "strides") and not hasattr(f, "data_ptr") else self.cameras[i][0])
+
+    def detect(self, frames, strides=None, device: bool = False):
+        self._set(frames, strides)
+        fn = lib().bd_batch_detect_device if device else lib().bd_batch_detect_host
+        rc = fn(self.handle, ctypes.cast(self._ptrs, _P), self._strides.ctypes.data,
+                self.out.ctypes.data, self.found.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"batch detect failed ({rc}): {last_error()}")
+        return self.found.copy(), self.out.copy()
+
+    def submit(self, frames, strides=None, device: bool = False) -> None:
+        self._set(frames, strides)
+        fn = lib().bd_batch_submit_device if device else lib().bd_batch_submit_host
+        rc = fn(self.handle, ctypes.cast(self._ptrs, _P), self._strides.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"batch submit failed ({rc}): {last_error()}")
+
+    def wait(self, copy: bool = True):
+        rc = lib().bd_batch_wait(self.handle, self.out.ctypes.data, self.found.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"batch wait failed ({rc}): {last_error()}")
+        return (self.found.copy(), self.out.copy()) if copy else (self.found, self.out)
+
+    def host_frame(self, i: int) -> np.ndarray:
+        w, h, _ = self.cameras[i]
+        p = lib().bd_batch_host_frame(self.handle, i)
+        return np.ctypeslib.as_array((ctypes.c_uint8 * (w * h)).from_address(p)).reshape(h, w)
+
+    def counts(self, i: int) -> np.ndarray:
+        c = np.zeros(5, dtype=np.uint32)
+        lib().bd_batch_counts(self.handle, i, c.ctypes.data)
+        return c
+
+    def last_gpu_ms(self) -> float:
+        return lib().bd_batch_last_gpu_ms(self.handle)
+
+    def device_bytes(self) -> int:
+        return lib().bd_batch_device_bytes(self.handle)
+
+    def stage(self, camera: int, name: str) -> np.ndarray:
+        return _stage(lib().bd_batch_debug_stage, self.handle, camera, name=name)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().bd_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()

@@ -1,0 +1,590 @@
+// C ABI and C++ API of bdcudatag on GB300.
+//
+// The fourteen reference symbols keep the reference's argument checks,
+// error messages, status codes, return values and statistics
+// (reference detector/src/detector.cpp:69-382, gpu_detector.cu:2100-2269);
+// detection itself runs on a one-frame batch Plan (engine.cu).  The batch
+// entry points of bdcudatag_gb300.h are new.
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bdcudatag/bdcudatag.h"
+#include "bdcudatag/bdcudatag_gb300.h"
+#include "bdcudatag/detector.hpp"
+#include "engine.h"
+#include "pipeline.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& message) { g_last_error = message; }
+
+struct FamilyInfo {
+    const char* name;
+    int bits_per_side;
+    int min_hamming;
+};
+
+const FamilyInfo kFamilies[2] = {{"tag36h11", 6, 11}, {"tag16h5", 4, 5}};
+
+bool valid_family(int family) { return family >= 0 && family < 2; }
+
+bool valid_dimensions(int width, int height) {
+    return width >= 16 && width <= BD_MAX_WIDTH && height >= 16 && height <= BD_MAX_HEIGHT;
+}
+
+int family_default_hamming(int family) { return family == BD_FAMILY_TAG36H11 ? 2 : 1; }
+
+bool config_size_ok(const bd_config* config) {
+    return !(config && config->struct_size != 0 && config->struct_size < sizeof(bd_config));
+}
+
+}  // namespace
+
+struct bd_detector {
+    bdgb::Plan* plan = nullptr;
+    int family = 0;
+    int width = 0;
+    int height = 0;
+    int max_detections = 0;
+    int max_candidates = 0;
+    // statistics (reference gpu_detector.cu:1829-1837)
+    uint64_t frames = 0;
+    float last_gpu_ms = 0.0f;
+    float average_gpu_ms = 0.0f;
+    float last_total_ms = 0.0f;
+    int last_candidates = 0;
+    int last_runs = 0;
+    int last_detections = 0;
+    int last_quads = 0;
+    int last_roi_rows = 0;
+};
+
+struct bd_batch {
+    bdgb::Plan* plan = nullptr;
+};
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// Copies results and updates statistics (reference Impl::finish
+// gpu_detector.cu:2100-2127).  The homography is already filled on the GPU.
+int finish(bd_detector* d, bd_detection* out, int out_capacity, float total_ms) {
+    const bdgb::Plan& plan = *d->plan;
+    const bdgb::FrameResultHeader* hdr = plan.result(0);
+    const int found = std::min(static_cast<int>(hdr->found[d->family]), d->max_detections);
+    const int written = std::min(found, std::max(out_capacity, 0));
+    if (written > 0 && out) {
+        std::memcpy(out, plan.detections(0, d->family), static_cast<size_t>(written) * sizeof(bd_detection));
+    }
+    d->last_candidates = std::min(static_cast<int>(hdr->counts[0]), d->max_candidates);
+    d->last_runs = static_cast<int>(hdr->counts[2]);
+    d->last_detections = found;
+    d->last_quads = static_cast<int>(hdr->counts[3]);
+    d->last_roi_rows = std::min(static_cast<int>(hdr->counts[4]) * bdgb::kTile, d->height);
+    const float gpu_ms = plan.last_gpu_ms();
+    d->last_gpu_ms = gpu_ms;
+    d->last_total_ms = total_ms;
+    d->average_gpu_ms = d->frames == 0 ? gpu_ms : 0.9f * d->average_gpu_ms + 0.1f * gpu_ms;
+    ++d->frames;
+    return found;
+}
+
+int check_detect_args(bd_detector* detector, const uint8_t* gray, int32_t stride, bd_detection* out,
+                      int32_t out_capacity, const char* null_message) {
+    if (!detector) {
+        set_error("null detector");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    if (!gray) {
+        set_error(null_message);
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    if (stride < detector->width) {
+        set_error("stride is smaller than the image width");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    if (out_capacity < 0 || (out_capacity > 0 && !out)) {
+        set_error("invalid output buffer");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    return BD_OK;
+}
+
+int32_t detect_common(bd_detector* detector, const uint8_t* gray, int32_t stride, bd_detection* out,
+                      int32_t out_capacity, bool device) {
+    const int bad = check_detect_args(detector, gray, stride, out, out_capacity,
+                                      device ? "null device image pointer" : "null image pointer");
+    if (bad != BD_OK) return bad;
+    bdgb::Plan& plan = *detector->plan;
+    const std::lock_guard<std::mutex> lock(plan.mutex());
+    const auto start = Clock::now();
+    std::string error;
+    const uint8_t* frames[1] = {gray};
+    const int32_t strides[1] = {stride};
+    const int rc = device ? plan.run_device(frames, strides, &error) : plan.run_host(frames, strides, &error);
+    if (rc != 0) {
+        set_error(error.empty() ? "CUDA detection failed" : error);
+        return BD_ERROR_CUDA;
+    }
+    const float total_ms = std::chrono::duration<float, std::milli>(Clock::now() - start).count();
+    return finish(detector, out, out_capacity, total_ms);
+}
+
+int32_t batch_collect(bd_batch* batch, bd_detection* out, int32_t* found) {
+    const bdgb::Plan& plan = *batch->plan;
+    const int md = plan.max_detections();
+    for (int i = 0; i < plan.frames(); ++i) {
+        for (int f = 0; f < 2; ++f) {
+            const bool on = (plan.frame(i).families >> f) & 1u;
+            const int n = on ? std::min(plan.found(i, f), md) : -1;
+            if (found) found[2 * i + f] = n;
+            if (out && n > 0) {
+                std::memcpy(out + (static_cast<size_t>(i) * 2 + f) * md, plan.detections(i, f),
+                            static_cast<size_t>(n) * sizeof(bd_detection));
+            }
+        }
+    }
+    return BD_OK;
+}
+
+int32_t batch_check(bd_batch* batch, const uint8_t* const* frames, const int32_t* strides) {
+    if (!batch) {
+        set_error("null batch");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    if (!frames || !strides) {
+        set_error("null frame or stride array");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < batch->plan->frames(); ++i) {
+        if (!frames[i]) {
+            set_error("null image pointer");
+            return BD_ERROR_INVALID_ARGUMENT;
+        }
+        if (strides[i] < batch->plan->frame(i).width) {
+            set_error("stride is smaller than the image width");
+            return BD_ERROR_INVALID_ARGUMENT;
+        }
+    }
+    return BD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t bd_api_version(void) { return BD_API_VERSION; }
+
+const char* bd_version_string(void) { return "bdcudatag 0.1.0"; }
+
+int32_t bd_family_count(void) { return 2; }
+
+const char* bd_family_name(int32_t family) {
+    if (!valid_family(family)) return nullptr;
+    return kFamilies[family].name;
+}
+
+int32_t bd_family_bits_per_side(int32_t family) {
+    if (!valid_family(family)) return -1;
+    return kFamilies[family].bits_per_side;
+}
+
+int32_t bd_family_min_hamming(int32_t family) {
+    if (!valid_family(family)) return -1;
+    return kFamilies[family].min_hamming;
+}
+
+int32_t bd_family_default_max_hamming(int32_t family) {
+    if (!valid_family(family)) return -1;
+    return family_default_hamming(family);
+}
+
+void bd_config_init(bd_config* config) {
+    if (!config) return;
+    std::memset(config, 0, sizeof(*config));
+    config->struct_size = sizeof(bd_config);
+    config->max_hamming = -1;
+    config->min_cluster_pixels = 24;
+    config->min_tag_pixels = 8;
+    config->max_detections = 64;
+    config->max_candidates = 0;
+    config->refine_edges = 1;
+    config->use_cuda_graph = 1;
+    config->min_decision_margin = 3.0f;
+    config->decode_sharpening = 0.25f;
+}
+
+bd_detector* bd_detector_create(int32_t family, int32_t width, int32_t height,
+                                const bd_config* config, int32_t* status_out) {
+    if (status_out) *status_out = BD_OK;
+    if (!valid_family(family)) {
+        set_error("unknown tag family");
+        if (status_out) *status_out = BD_ERROR_INVALID_ARGUMENT;
+        return nullptr;
+    }
+    if (!valid_dimensions(width, height)) {
+        set_error("image dimensions out of range (16..8192 x 16..16384)");
+        if (status_out) *status_out = BD_ERROR_INVALID_ARGUMENT;
+        return nullptr;
+    }
+    if (!config_size_ok(config)) {
+        set_error("bd_config.struct_size is too small for this library version");
+        if (status_out) *status_out = BD_ERROR_INVALID_ARGUMENT;
+        return nullptr;
+    }
+    const bdgb::PlanConfig pc = bdgb::resolve_config(config);
+    bdgb::PlanFrame frame;
+    frame.width = width;
+    frame.height = height;
+    frame.families = 1u << family;
+    std::string error;
+    bdgb::Plan* plan = bdgb::Plan::create({frame}, pc, &error);
+    if (!plan) {
+        set_error(error.empty() ? "failed to create CUDA detector" : error);
+        if (status_out) *status_out = BD_ERROR_CUDA;
+        return nullptr;
+    }
+    bd_detector* detector = new (std::nothrow) bd_detector();
+    if (!detector) {
+        delete plan;
+        set_error("out of memory allocating detector handle");
+        if (status_out) *status_out = BD_ERROR_OUT_OF_MEMORY;
+        return nullptr;
+    }
+    detector->plan = plan;
+    detector->family = family;
+    detector->width = width;
+    detector->height = height;
+    detector->max_detections = pc.max_detections;
+    detector->max_candidates = plan->max_candidates(0);
+    return detector;
+}
+
+void bd_detector_destroy(bd_detector* detector) {
+    if (!detector) return;
+    delete detector->plan;
+    delete detector;
+}
+
+int32_t bd_detector_detect_host(bd_detector* detector, const uint8_t* gray, int32_t stride,
+                                bd_detection* out, int32_t out_capacity) {
+    return detect_common(detector, gray, stride, out, out_capacity, false);
+}
+
+int32_t bd_detector_detect_device(bd_detector* detector, const uint8_t* gray_device,
+                                  int32_t stride, bd_detection* out, int32_t out_capacity) {
+    return detect_common(detector, gray_device, stride, out, out_capacity, true);
+}
+
+void bd_detector_get_stats(bd_detector* detector, bd_stats* out) {
+    if (!detector || !out) return;
+    const std::lock_guard<std::mutex> lock(detector->plan->mutex());
+    out->frames = detector->frames;
+    out->last_gpu_ms = detector->last_gpu_ms;
+    out->average_gpu_ms = detector->average_gpu_ms;
+    out->last_total_ms = detector->last_total_ms;
+    out->runs = detector->last_runs;
+    out->candidates = detector->last_candidates;
+    out->detections = detector->last_detections;
+    out->quads = detector->last_quads;
+    out->roi_rows = detector->last_roi_rows;
+}
+
+const char* bd_last_error(void) { return g_last_error.c_str(); }
+
+// --- batches ------------------------------------------------------------------
+
+bd_batch* bd_batch_create(const bd_camera* cameras, int32_t count, const bd_config* config,
+                          int32_t* status_out) {
+    if (status_out) *status_out = BD_OK;
+    if (!cameras || count < 1 || count > BD_BATCH_MAX_CAMERAS) {
+        set_error("a batch needs 1 to 64 cameras");
+        if (status_out) *status_out = BD_ERROR_INVALID_ARGUMENT;
+        return nullptr;
+    }
+    if (!config_size_ok(config)) {
+        set_error("bd_config.struct_size is too small for this library version");
+        if (status_out) *status_out = BD_ERROR_INVALID_ARGUMENT;
+        return nullptr;
+    }
+    std::vector<bdgb::PlanFrame> frames(count);
+    for (int i = 0; i < count; ++i) {
+        if (!valid_dimensions(cameras[i].width, cameras[i].height)) {
+            set_error("image dimensions out of range (16..8192 x 16..16384)");
+            if (status_out) *status_out = BD_ERROR_INVALID_ARGUMENT;
+            return nullptr;
+        }
+        if ((cameras[i].families & 3u) == 0 || (cameras[i].families & ~3u) != 0) {
+            set_error("camera family mask must select tag36h11 and/or tag16h5");
+            if (status_out) *status_out = BD_ERROR_INVALID_ARGUMENT;
+            return nullptr;
+        }
+        frames[i].width = cameras[i].width;
+        frames[i].height = cameras[i].height;
+        frames[i].families = cameras[i].families;
+    }
+    std::string error;
+    bdgb::Plan* plan = bdgb::Plan::create(frames, bdgb::resolve_config(config), &error);
+    if (!plan) {
+        set_error(error.empty() ? "failed to create CUDA batch" : error);
+        if (status_out) *status_out = BD_ERROR_CUDA;
+        return nullptr;
+    }
+    bd_batch* batch = new (std::nothrow) bd_batch();
+    if (!batch) {
+        delete plan;
+        set_error("out of memory allocating batch handle");
+        if (status_out) *status_out = BD_ERROR_OUT_OF_MEMORY;
+        return nullptr;
+    }
+    batch->plan = plan;
+    return batch;
+}
+
+void bd_batch_destroy(bd_batch* batch) {
+    if (!batch) return;
+    delete batch->plan;
+    delete batch;
+}
+
+int32_t bd_batch_camera_count(const bd_batch* batch) { return batch ? batch->plan->frames() : 0; }
+
+int32_t bd_batch_max_detections(const bd_batch* batch) {
+    return batch ? batch->plan->max_detections() : 0;
+}
+
+int64_t bd_batch_device_bytes(const bd_batch* batch) {
+    return batch ? static_cast<int64_t>(batch->plan->device_bytes()) : 0;
+}
+
+int32_t bd_batch_submit_host(bd_batch* batch, const uint8_t* const* frames, const int32_t* strides) {
+    const int bad = batch_check(batch, frames, strides);
+    if (bad != BD_OK) return bad;
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    std::string error;
+    if (batch->plan->submit_host(frames, strides, &error) != 0) {
+        set_error(error);
+        return BD_ERROR_CUDA;
+    }
+    return BD_OK;
+}
+
+int32_t bd_batch_submit_device(bd_batch* batch, const uint8_t* const* frames,
+                               const int32_t* strides) {
+    const int bad = batch_check(batch, frames, strides);
+    if (bad != BD_OK) return bad;
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    std::string error;
+    if (batch->plan->submit_device(frames, strides, &error) != 0) {
+        set_error(error);
+        return BD_ERROR_CUDA;
+    }
+    return BD_OK;
+}
+
+int32_t bd_batch_wait(bd_batch* batch, bd_detection* out, int32_t* found) {
+    if (!batch) {
+        set_error("null batch");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    std::string error;
+    if (batch->plan->wait(&error) != 0) {
+        set_error(error);
+        return BD_ERROR_CUDA;
+    }
+    return batch_collect(batch, out, found);
+}
+
+int32_t bd_batch_detect_host(bd_batch* batch, const uint8_t* const* frames, const int32_t* strides,
+                             bd_detection* out, int32_t* found) {
+    const int rc = bd_batch_submit_host(batch, frames, strides);
+    if (rc != BD_OK) return rc;
+    return bd_batch_wait(batch, out, found);
+}
+
+int32_t bd_batch_detect_device(bd_batch* batch, const uint8_t* const* frames,
+                               const int32_t* strides, bd_detection* out, int32_t* found) {
+    const int rc = bd_batch_submit_device(batch, frames, strides);
+    if (rc != BD_OK) return rc;
+    return bd_batch_wait(batch, out, found);
+}
+
+uint8_t* bd_batch_host_frame(bd_batch* batch, int32_t camera) {
+    if (!batch || camera < 0 || camera >= batch->plan->frames()) return nullptr;
+    return batch->plan->host_frame(camera);
+}
+
+float bd_batch_last_gpu_ms(const bd_batch* batch) { return batch ? batch->plan->last_gpu_ms() : 0.0f; }
+
+int32_t bd_batch_counts(const bd_batch* batch, int32_t camera, uint32_t counts[5]) {
+    if (!batch || !counts || camera < 0 || camera >= batch->plan->frames()) {
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    std::memcpy(counts, batch->plan->result(camera)->counts, 5 * sizeof(uint32_t));
+    return BD_OK;
+}
+
+int64_t bd_batch_debug_stage(bd_batch* batch, int32_t camera, const char* name, void* dst,
+                             int64_t dst_bytes) {
+    if (!batch) return -1;
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    return batch->plan->copy_stage(camera, name, dst, dst_bytes);
+}
+
+int64_t bd_detector_debug_stage(bd_detector* detector, const char* name, void* dst,
+                                int64_t dst_bytes) {
+    if (!detector) return -1;
+    const std::lock_guard<std::mutex> lock(detector->plan->mutex());
+    return detector->plan->copy_stage(0, name, dst, dst_bytes);
+}
+
+}  // extern "C"
+
+// --- C++ API (reference detector.cpp:229-382) ----------------------------------
+
+namespace bdcudatag {
+
+struct Detector::Impl {
+    bd_detector* handle = nullptr;
+    int max_detections = 0;
+    std::vector<bd_detection> scratch;
+    // Serialises callers that share the scratch buffer.
+    std::mutex mutex;
+};
+
+Detector::Detector(Family family, int width, int height, const DetectorConfig& config)
+    : family_(family), width_(width), height_(height) {
+    bd_config native;
+    bd_config_init(&native);
+    native.max_hamming = config.max_hamming;
+    native.min_cluster_pixels = config.min_cluster_pixels;
+    native.min_tag_pixels = config.min_tag_pixels;
+    native.max_detections = config.max_detections;
+    native.max_candidates = config.max_candidates;
+    native.refine_edges = config.refine_edges ? 1 : 0;
+    native.use_cuda_graph = config.use_cuda_graph ? 1 : 0;
+    native.min_decision_margin = config.min_decision_margin;
+    native.decode_sharpening = config.decode_sharpening;
+    int32_t status = BD_OK;
+    impl_ = new Impl();
+    impl_->handle = bd_detector_create(static_cast<int32_t>(family), width, height, &native, &status);
+    if (!impl_->handle) {
+        const std::string message = bd_last_error();
+        delete impl_;
+        impl_ = nullptr;
+        throw std::runtime_error(message.empty() ? "failed to create bdcudatag detector" : message);
+    }
+    impl_->max_detections = std::min(std::max(native.max_detections, 1), 256);
+    impl_->scratch.resize(static_cast<size_t>(impl_->max_detections));
+}
+
+Detector::~Detector() {
+    if (!impl_) return;
+    if (impl_->handle) bd_detector_destroy(impl_->handle);
+    delete impl_;
+}
+
+Detector::Detector(Detector&& other) noexcept
+    : impl_(other.impl_), family_(other.family_), width_(other.width_), height_(other.height_) {
+    other.impl_ = nullptr;
+}
+
+Detector& Detector::operator=(Detector&& other) noexcept {
+    if (this == &other) return *this;
+    if (impl_) {
+        if (impl_->handle) bd_detector_destroy(impl_->handle);
+        delete impl_;
+    }
+    impl_ = other.impl_;
+    family_ = other.family_;
+    width_ = other.width_;
+    height_ = other.height_;
+    other.impl_ = nullptr;
+    return *this;
+}
+
+namespace {
+
+void to_detections(const bd_detection* src, int count, Detection* out) {
+    for (int i = 0; i < count; ++i) {
+        Detection& dst = out[i];
+        dst.id = src[i].id;
+        dst.hamming = src[i].hamming;
+        dst.decision_margin = src[i].decision_margin;
+        for (int k = 0; k < 4; ++k) {
+            dst.corners[static_cast<size_t>(k)][0] = src[i].corners[k * 2 + 0];
+            dst.corners[static_cast<size_t>(k)][1] = src[i].corners[k * 2 + 1];
+        }
+        for (int k = 0; k < 9; ++k) dst.homography[static_cast<size_t>(k)] = src[i].homography[k];
+    }
+}
+
+}  // namespace
+
+int Detector::detect(const uint8_t* gray, int stride, Detection* out, int out_capacity) {
+    if (!impl_) throw std::runtime_error("detector has been moved from");
+    if (out_capacity < 0 || (out_capacity > 0 && !out)) {
+        throw std::invalid_argument("invalid detection output buffer");
+    }
+    if (out_capacity > impl_->max_detections) out_capacity = impl_->max_detections;
+    const std::lock_guard<std::mutex> lock(impl_->mutex);
+    const int count = bd_detector_detect_host(impl_->handle, gray, stride, impl_->scratch.data(),
+                                              out_capacity);
+    if (count < 0) throw std::runtime_error(bd_last_error());
+    const int written = std::min(count, out_capacity);
+    to_detections(impl_->scratch.data(), written, out);
+    return written;
+}
+
+std::vector<Detection> Detector::detect(const uint8_t* gray, int stride) {
+    if (!impl_) throw std::runtime_error("detector has been moved from");
+    std::vector<Detection> result(static_cast<size_t>(impl_->max_detections));
+    const int count = detect(gray, stride, result.data(), impl_->max_detections);
+    result.resize(static_cast<size_t>(count));
+    return result;
+}
+
+int Detector::detectDevice(const uint8_t* gray_device, int stride, Detection* out, int out_capacity) {
+    if (!impl_) throw std::runtime_error("detector has been moved from");
+    if (out_capacity < 0 || (out_capacity > 0 && !out)) {
+        throw std::invalid_argument("invalid detection output buffer");
+    }
+    if (out_capacity > impl_->max_detections) out_capacity = impl_->max_detections;
+    const std::lock_guard<std::mutex> lock(impl_->mutex);
+    const int count = bd_detector_detect_device(impl_->handle, gray_device, stride,
+                                                impl_->scratch.data(), out_capacity);
+    if (count < 0) throw std::runtime_error(bd_last_error());
+    const int written = std::min(count, out_capacity);
+    to_detections(impl_->scratch.data(), written, out);
+    return written;
+}
+
+Stats Detector::stats() const {
+    if (!impl_) return {};
+    const std::lock_guard<std::mutex> lock(impl_->mutex);
+    bd_stats native;
+    bd_detector_get_stats(impl_->handle, &native);
+    Stats out;
+    out.frames = native.frames;
+    out.last_gpu_ms = native.last_gpu_ms;
+    out.average_gpu_ms = native.average_gpu_ms;
+    out.last_total_ms = native.last_total_ms;
+    out.runs = native.runs;
+    out.candidates = native.candidates;
+    out.detections = native.detections;
+    out.quads = native.quads;
+    out.roi_rows = native.roi_rows;
+    return out;
+}
+
+}  // namespace bdcudatag

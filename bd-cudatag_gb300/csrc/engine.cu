@@ -1,0 +1,467 @@
+// Host engine: arena allocation, pinned staging, CUDA graphs and result
+// copies for a plan of frames (the reference's GpuDetector::Impl,
+// gpu_detector.cu:1784-2254, generalised from one frame to a batch).
+//
+// Memory: one cudaMalloc per plan holds every per-frame buffer, carved at
+// 256-byte alignment; the per-frame state records and the result records
+// are each contiguous, so a batch costs one memset node and one result copy.
+// Detect calls never allocate.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <sstream>
+
+#include "engine.h"
+#include "pipeline.cuh"
+
+namespace bdgb {
+
+namespace {
+
+std::string cuda_error(const char* what, cudaError_t status) {
+    std::ostringstream ss;
+    ss << what << ": " << cudaGetErrorString(status);
+    return ss.str();
+}
+
+int next_power_of_two(int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+PlanConfig resolve_config(const bd_config* config) {
+    bd_config c;
+    bd_config_init(&c);
+    if (config) c = *config;
+    PlanConfig p;
+    for (int f = 0; f < 2; ++f) {
+        p.max_hamming[f] = c.max_hamming >= 0 ? std::min(c.max_hamming, 3) : (f == 0 ? 2 : 1);
+    }
+    p.min_cluster_pixels = std::max(c.min_cluster_pixels, 1);
+    p.min_tag_pixels = std::max(c.min_tag_pixels, 4);
+    p.max_detections = std::min(std::max(c.max_detections, 1), kMaxDetectionsCap);
+    p.max_candidates = c.max_candidates;
+    p.refine_edges = c.refine_edges != 0;
+    p.use_graph = c.use_cuda_graph != 0;
+    p.min_decision_margin = c.min_decision_margin;
+    p.decode_sharpening = c.decode_sharpening;
+    return p;
+}
+
+int auto_max_candidates(int width, int height, int configured) {
+    if (configured > 0) return std::min(std::max(configured, 16), 1024);
+    return std::min(std::max(next_power_of_two((width * height) / 4096) * 3 / 2, 96), 1024);
+}
+
+struct Plan::Impl {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_stop = nullptr;
+    void* arena = nullptr;
+    BatchDesc host_desc{};
+    BatchDesc* dev_desc = nullptr;
+    FrameIO* io_fixed = nullptr;     // device: arena frame buffers
+    FrameIO* io_caller = nullptr;    // device: caller pointers, device path
+    FrameIO* io_staging = nullptr;   // pinned
+    uint8_t* frames_dev = nullptr;
+    uint8_t* frames_pinned = nullptr;
+    size_t frame_bytes = 0;
+    std::vector<size_t> frame_offset;
+    FrameState* states = nullptr;
+    size_t states_bytes = 0;
+    uint8_t* results_dev = nullptr;
+    uint8_t* results_pinned = nullptr;
+    size_t results_bytes = 0;
+    size_t result_stride = 0;
+    cudaGraphExec_t graph_host = nullptr;
+    cudaGraphExec_t graph_device = nullptr;
+    bool pending = false;
+
+    ~Impl() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph_host) cudaGraphExecDestroy(graph_host);
+        if (graph_device) cudaGraphExecDestroy(graph_device);
+        if (ev_start) cudaEventDestroy(ev_start);
+        if (ev_stop) cudaEventDestroy(ev_stop);
+        if (stream) cudaStreamDestroy(stream);
+        if (arena) cudaFree(arena);
+        if (frames_pinned) cudaFreeHost(frames_pinned);
+        if (results_pinned) cudaFreeHost(results_pinned);
+        if (io_staging) cudaFreeHost(io_staging);
+    }
+
+    void enqueue_host() {
+        cudaMemcpyAsync(frames_dev, frames_pinned, frame_bytes, cudaMemcpyHostToDevice, stream);
+        cudaMemsetAsync(states, 0, states_bytes, stream);
+        enqueue_pipeline(dev_desc, host_desc, io_fixed, stream);
+        cudaMemcpyAsync(results_pinned, results_dev, results_bytes, cudaMemcpyDeviceToHost, stream);
+    }
+
+    void enqueue_device() {
+        cudaMemcpyAsync(io_caller, io_staging, sizeof(FrameIO) * host_desc.frames,
+                        cudaMemcpyHostToDevice, stream);
+        cudaMemsetAsync(states, 0, states_bytes, stream);
+        enqueue_pipeline(dev_desc, host_desc, io_caller, stream);
+        cudaMemcpyAsync(results_pinned, results_dev, results_bytes, cudaMemcpyDeviceToHost, stream);
+    }
+
+    bool capture(bool device_mode, cudaGraphExec_t* out) {
+        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (device_mode) enqueue_device(); else enqueue_host();
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamEndCapture(stream, &graph) != cudaSuccess || !graph) {
+            cudaGetLastError();
+            return false;
+        }
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t st = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (st != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        *out = exec;
+        return true;
+    }
+};
+
+Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& config,
+                   std::string* error) {
+    if (frames.empty() || frames.size() > static_cast<size_t>(kMaxFrames)) {
+        if (error) *error = "a plan holds 1 to 64 frames";
+        return nullptr;
+    }
+    for (const PlanFrame& f : frames) {
+        if (f.width < 16 || f.width > BD_MAX_WIDTH || f.height < 16 || f.height > BD_MAX_HEIGHT) {
+            if (error) *error = "image dimensions out of range (16..8192 x 16..16384)";
+            return nullptr;
+        }
+        if ((f.families & 3u) == 0 || (f.families & ~3u) != 0) {
+            if (error) *error = "family mask must select tag36h11 and/or tag16h5";
+            return nullptr;
+        }
+    }
+    Plan* plan = new Plan();
+    plan->frames_ = frames;
+    plan->config_ = config;
+    plan->impl_ = new Impl();
+    Impl& im = *plan->impl_;
+    auto fail = [&](const std::string& msg) -> Plan* {
+        if (error) *error = msg;
+        delete plan;
+        return nullptr;
+    };
+    cudaError_t st = cudaGetDevice(&im.device);
+    if (st != cudaSuccess) return fail(cuda_error("cudaGetDevice", st));
+
+    const int nf = static_cast<int>(frames.size());
+    const int md = config.max_detections;
+    // --- sizes and arena layout ---
+    struct Carve {
+        size_t off = 0;
+        size_t take(size_t bytes) {
+            const size_t at = off;
+            off = align_up(off + std::max<size_t>(bytes, 1), 256);
+            return at;
+        }
+    } carve;
+    BatchDesc& hd = im.host_desc;
+    std::memset(&hd, 0, sizeof(hd));
+    hd.frames = nf;
+    std::vector<size_t> off_frame(nf), off_tmin(nf), off_tmax(nf), off_lo(nf), off_hi(nf),
+        off_bits(nf), off_rc(nf), off_runs(nf), off_parent(nf), off_area(nf), off_bbox(nf),
+        off_meta(nf), off_bands(nf), off_cands(nf), off_hull(nf), off_quads(nf), off_dec(nf);
+    im.frame_offset.resize(nf);
+    size_t frame_total = 0;
+    for (int i = 0; i < nf; ++i) {
+        im.frame_offset[i] = frame_total;
+        frame_total += align_up(static_cast<size_t>(frames[i].width) * frames[i].height, 256);
+    }
+    im.frame_bytes = frame_total;
+    const size_t frames_at = carve.take(frame_total);
+    im.states_bytes = sizeof(FrameState) * nf;
+    const size_t states_at = carve.take(im.states_bytes);
+    im.result_stride = align_up(result_bytes(md), 256);
+    im.results_bytes = im.result_stride * nf;
+    const size_t results_at = carve.take(im.results_bytes);
+    const size_t desc_at = carve.take(sizeof(BatchDesc));
+    const size_t io_fixed_at = carve.take(sizeof(FrameIO) * nf);
+    const size_t io_caller_at = carve.take(sizeof(FrameIO) * nf);
+    int bands = 0;
+    for (int i = 0; i < nf; ++i) {
+        FrameDesc& d = hd.f[i];
+        const PlanFrame& f = frames[i];
+        d.width = f.width;
+        d.height = f.height;
+        d.tile_w = (f.width + kTile - 1) / kTile;
+        d.tile_h = (f.height + kTile - 1) / kTile;
+        d.words = (f.width + 31) / 32;
+        d.row_cap = f.width / 2 + 2;
+        d.max_candidates = auto_max_candidates(f.width, f.height, config.max_candidates);
+        d.max_detections = md;
+        d.families = f.families;
+        d.min_cluster_pixels = config.min_cluster_pixels;
+        d.min_tag_pixels = config.min_tag_pixels;
+        d.refine_edges = config.refine_edges ? 1 : 0;
+        d.max_hamming[0] = config.max_hamming[0];
+        d.max_hamming[1] = config.max_hamming[1];
+        d.min_margin = config.min_decision_margin;
+        d.sharpening = config.decode_sharpening;
+        const size_t T = static_cast<size_t>(d.tile_w) * d.tile_h;
+        const size_t slots = static_cast<size_t>(f.height) * d.row_cap;
+        const size_t mc = static_cast<size_t>(d.max_candidates);
+        hd.band_prefix[i] = bands;
+        bands += d.tile_h;
+        off_tmin[i] = carve.take(T);
+        off_tmax[i] = carve.take(T);
+        off_lo[i] = carve.take(sizeof(int32_t) * d.tile_h);
+        off_hi[i] = carve.take(sizeof(int32_t) * d.tile_h);
+        off_bits[i] = carve.take(sizeof(uint32_t) * d.words * f.height);
+        off_rc[i] = carve.take(sizeof(uint32_t) * f.height);
+        off_runs[i] = carve.take(sizeof(uint32_t) * slots);
+        off_parent[i] = carve.take(sizeof(uint32_t) * slots);
+        off_area[i] = carve.take(sizeof(uint32_t) * slots);
+        off_bbox[i] = carve.take(sizeof(uint32_t) * 4 * slots);
+        off_meta[i] = carve.take(sizeof(uint32_t) * slots);
+        off_bands[i] = carve.take(sizeof(uint32_t) * 64 * d.tile_h);
+        off_cands[i] = carve.take(sizeof(uint32_t) * mc);
+        off_hull[i] = carve.take(sizeof(float) * 8 * mc);
+        off_quads[i] = carve.take(sizeof(float) * 16 * mc);
+        off_dec[i] = carve.take(sizeof(DecodeOut) * 2 * mc);
+    }
+    hd.band_prefix[nf] = bands;
+    hd.total_bands = bands;
+    plan->arena_bytes_ = carve.off;
+
+    st = cudaMalloc(&im.arena, carve.off);
+    if (st != cudaSuccess) {
+        cudaGetLastError();
+        return fail(cuda_error("cudaMalloc", st));
+    }
+    uint8_t* base = static_cast<uint8_t*>(im.arena);
+    im.frames_dev = base + frames_at;
+    im.states = reinterpret_cast<FrameState*>(base + states_at);
+    im.results_dev = base + results_at;
+    im.dev_desc = reinterpret_cast<BatchDesc*>(base + desc_at);
+    im.io_fixed = reinterpret_cast<FrameIO*>(base + io_fixed_at);
+    im.io_caller = reinterpret_cast<FrameIO*>(base + io_caller_at);
+    std::vector<FrameIO> fixed(nf);
+    for (int i = 0; i < nf; ++i) {
+        FrameDesc& d = hd.f[i];
+        d.tile_min = base + off_tmin[i];
+        d.tile_max = base + off_tmax[i];
+        d.row_lo = reinterpret_cast<int32_t*>(base + off_lo[i]);
+        d.row_hi = reinterpret_cast<int32_t*>(base + off_hi[i]);
+        d.bits = reinterpret_cast<uint32_t*>(base + off_bits[i]);
+        d.row_count = reinterpret_cast<uint32_t*>(base + off_rc[i]);
+        d.runs = reinterpret_cast<uint32_t*>(base + off_runs[i]);
+        d.parent = reinterpret_cast<uint32_t*>(base + off_parent[i]);
+        d.area = reinterpret_cast<uint32_t*>(base + off_area[i]);
+        d.bbox = reinterpret_cast<uint32_t*>(base + off_bbox[i]);
+        d.cand_meta = reinterpret_cast<uint32_t*>(base + off_meta[i]);
+        d.band_bins = reinterpret_cast<uint32_t*>(base + off_bands[i]);
+        d.candidates = reinterpret_cast<uint32_t*>(base + off_cands[i]);
+        d.state = im.states + i;
+        d.hull_quads = reinterpret_cast<float*>(base + off_hull[i]);
+        d.quads = reinterpret_cast<float*>(base + off_quads[i]);
+        d.decodes = reinterpret_cast<DecodeOut*>(base + off_dec[i]);
+        d.result = reinterpret_cast<FrameResultHeader*>(im.results_dev + im.result_stride * i);
+        fixed[i].gray = im.frames_dev + im.frame_offset[i];
+        fixed[i].stride = frames[i].width;
+    }
+    st = cudaHostAlloc(reinterpret_cast<void**>(&im.frames_pinned), frame_total, cudaHostAllocPortable);
+    if (st == cudaSuccess)
+        st = cudaHostAlloc(reinterpret_cast<void**>(&im.results_pinned), im.results_bytes,
+                           cudaHostAllocPortable);
+    if (st == cudaSuccess)
+        st = cudaHostAlloc(reinterpret_cast<void**>(&im.io_staging), sizeof(FrameIO) * nf,
+                           cudaHostAllocPortable);
+    if (st != cudaSuccess) {
+        cudaGetLastError();
+        return fail(cuda_error("cudaHostAlloc", st));
+    }
+    std::memset(im.results_pinned, 0, im.results_bytes);
+    st = cudaStreamCreateWithFlags(&im.stream, cudaStreamNonBlocking);
+    if (st == cudaSuccess) st = cudaEventCreate(&im.ev_start);
+    if (st == cudaSuccess) st = cudaEventCreate(&im.ev_stop);
+    if (st != cudaSuccess) return fail(cuda_error("cudaStreamCreate", st));
+    st = cudaMemcpy(im.dev_desc, &hd, sizeof(BatchDesc), cudaMemcpyHostToDevice);
+    if (st == cudaSuccess)
+        st = cudaMemcpy(im.io_fixed, fixed.data(), sizeof(FrameIO) * nf, cudaMemcpyHostToDevice);
+    if (st == cudaSuccess) st = cudaMemset(im.frames_dev, 0, frame_total);
+    if (st == cudaSuccess) st = cudaMemset(im.results_dev, 0, im.results_bytes);
+    if (st != cudaSuccess) return fail(cuda_error("cudaMemcpy(plan)", st));
+    for (int i = 0; i < nf; ++i) {
+        im.io_staging[i].gray = fixed[i].gray;
+        im.io_staging[i].stride = fixed[i].stride;
+    }
+    if (config.use_graph) {
+        // A failed capture falls back to direct launches (reference
+        // gpu_detector.cu:2051-2056).
+        if (!im.capture(false, &im.graph_host)) im.graph_host = nullptr;
+        if (!im.capture(true, &im.graph_device)) im.graph_device = nullptr;
+    }
+    return plan;
+}
+
+Plan::~Plan() { delete impl_; }
+
+int Plan::max_candidates(int frame) const { return impl_->host_desc.f[frame].max_candidates; }
+
+uint8_t* Plan::host_frame(int i) { return impl_->frames_pinned + impl_->frame_offset[i]; }
+
+int Plan::submit_host(const uint8_t* const* frames, const int32_t* strides, std::string* error) {
+    Impl& im = *impl_;
+    if (im.pending) {
+        if (error) *error = "a batch is already in flight";
+        return -1;
+    }
+    for (int i = 0; i < this->frames(); ++i) {
+        const int w = frames_[i].width, h = frames_[i].height;
+        uint8_t* dst = im.frames_pinned + im.frame_offset[i];
+        if (!frames[i]) {
+            if (error) *error = "null image pointer";
+            return -1;
+        }
+        if (frames[i] == dst) continue;  // rendered in place
+        if (strides[i] == w) {
+            std::memcpy(dst, frames[i], static_cast<size_t>(w) * h);
+        } else {
+            for (int y = 0; y < h; ++y) {
+                std::memcpy(dst + static_cast<size_t>(y) * w,
+                            frames[i] + static_cast<size_t>(y) * strides[i], w);
+            }
+        }
+    }
+    cudaEventRecord(im.ev_start, im.stream);
+    if (im.graph_host) {
+        const cudaError_t st = cudaGraphLaunch(im.graph_host, im.stream);
+        if (st != cudaSuccess) {
+            if (error) *error = cuda_error("cudaGraphLaunch", st);
+            return -1;
+        }
+    } else {
+        im.enqueue_host();
+    }
+    cudaEventRecord(im.ev_stop, im.stream);
+    im.pending = true;
+    return 0;
+}
+
+int Plan::submit_device(const uint8_t* const* frames, const int32_t* strides, std::string* error) {
+    Impl& im = *impl_;
+    if (im.pending) {
+        if (error) *error = "a batch is already in flight";
+        return -1;
+    }
+    for (int i = 0; i < this->frames(); ++i) {
+        if (!frames[i]) {
+            if (error) *error = "null device image pointer";
+            return -1;
+        }
+        im.io_staging[i].gray = frames[i];
+        im.io_staging[i].stride = strides[i];
+    }
+    cudaEventRecord(im.ev_start, im.stream);
+    if (im.graph_device) {
+        const cudaError_t st = cudaGraphLaunch(im.graph_device, im.stream);
+        if (st != cudaSuccess) {
+            if (error) *error = cuda_error("cudaGraphLaunch", st);
+            return -1;
+        }
+    } else {
+        im.enqueue_device();
+    }
+    cudaEventRecord(im.ev_stop, im.stream);
+    im.pending = true;
+    return 0;
+}
+
+int Plan::wait(std::string* error) {
+    Impl& im = *impl_;
+    if (!im.pending) return 0;
+    im.pending = false;
+    const cudaError_t st = cudaEventSynchronize(im.ev_stop);
+    if (st != cudaSuccess) {
+        if (error) *error = cuda_error("cudaEventSynchronize", st);
+        return -1;
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, im.ev_start, im.ev_stop);
+    last_gpu_ms_ = ms;
+    const cudaError_t late = cudaGetLastError();
+    if (late != cudaSuccess) {
+        if (error) *error = cuda_error("CUDA launch", late);
+        return -1;
+    }
+    return 0;
+}
+
+int Plan::run_host(const uint8_t* const* frames, const int32_t* strides, std::string* error) {
+    if (submit_host(frames, strides, error) != 0) return -1;
+    return wait(error);
+}
+
+int Plan::run_device(const uint8_t* const* frames, const int32_t* strides, std::string* error) {
+    if (submit_device(frames, strides, error) != 0) return -1;
+    return wait(error);
+}
+
+const FrameResultHeader* Plan::result(int frame) const {
+    return reinterpret_cast<const FrameResultHeader*>(impl_->results_pinned +
+                                                      impl_->result_stride * frame);
+}
+
+const bd_detection* Plan::detections(int frame, int family) const {
+    return result_detections(const_cast<FrameResultHeader*>(result(frame))) +
+           static_cast<size_t>(family) * config_.max_detections;
+}
+
+int Plan::found(int frame, int family) const {
+    return static_cast<int>(result(frame)->found[family]);
+}
+
+int64_t Plan::copy_stage(int frame, const char* name, void* dst, int64_t dst_bytes) {
+    Impl& im = *impl_;
+    if (frame < 0 || frame >= frames() || !name) return -1;
+    const FrameDesc& d = im.host_desc.f[frame];
+    const size_t T = static_cast<size_t>(d.tile_w) * d.tile_h;
+    const size_t slots = static_cast<size_t>(d.height) * d.row_cap;
+    const size_t mc = static_cast<size_t>(d.max_candidates);
+    const std::string n(name);
+    const void* src = nullptr;
+    size_t bytes = 0;
+    if (n == "tile_min") { src = d.tile_min; bytes = T; }
+    else if (n == "tile_max") { src = d.tile_max; bytes = T; }
+    else if (n == "bits") { src = d.bits; bytes = sizeof(uint32_t) * d.words * d.height; }
+    else if (n == "row_count") { src = d.row_count; bytes = sizeof(uint32_t) * d.height; }
+    else if (n == "runs") { src = d.runs; bytes = sizeof(uint32_t) * slots; }
+    else if (n == "label") { src = d.parent; bytes = sizeof(uint32_t) * slots; }
+    else if (n == "area") { src = d.area; bytes = sizeof(uint32_t) * slots; }
+    else if (n == "bbox") { src = d.bbox; bytes = sizeof(uint32_t) * 4 * slots; }
+    else if (n == "candidates") { src = d.candidates; bytes = sizeof(uint32_t) * mc; }
+    else if (n == "hull_quads") { src = d.hull_quads; bytes = sizeof(float) * 8 * mc; }
+    else if (n == "quads") { src = d.quads; bytes = sizeof(float) * 16 * mc; }
+    else if (n == "decodes") { src = d.decodes; bytes = sizeof(DecodeOut) * 2 * mc; }
+    else if (n == "state") { src = d.state; bytes = sizeof(FrameState); }
+    else return -1;
+    if (dst && dst_bytes > 0) {
+        cudaStreamSynchronize(im.stream);
+        const size_t n_copy = std::min(bytes, static_cast<size_t>(dst_bytes));
+        if (cudaMemcpy(dst, src, n_copy, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    }
+    return static_cast<int64_t>(bytes);
+}
+
+}  // namespace bdgb

@@ -27,14 +27,17 @@ def parse(text: str, name: str) -> list[int]:
 
 
 def emit(name: str, bits: int, values: list[int]) -> str:
+    """A macro holding the initializer list, so host and __device__ arrays
+    can both be defined from it."""
     width = (bits * bits + 3) // 4
     lines = [f"// {len(values)} codewords, {bits}x{bits} data cells, row-major, MSB = top-left cell",
-             f"static const uint64_t {name}[{len(values)}] = {{"]
+             f"#define {name}_COUNT {len(values)}",
+             f"#define {name} \\"]
     per_line = 6 if bits == 6 else 8
     for i in range(0, len(values), per_line):
         chunk = values[i:i + per_line]
-        lines.append("    " + " ".join(f"0x{v:0{width}x}ull," for v in chunk))
-    lines.append("};")
+        lines.append("    " + " ".join(f"0x{v:0{width}x}ull," for v in chunk) + " \\")
+    lines[-1] = lines[-1][:-2]
     return "\n".join(lines)
 
 
@@ -47,8 +50,9 @@ def main() -> None:
         "// Generated by gen_families.py; do not edit.\n"
         "// Tag family codewords: data of the AprilTag project,\n"
         "// Copyright (C) 2013-2016, The Regents of The University of Michigan,\n"
-        "// BSD 2-Clause license (third_party/APRILTAG_LICENSE.md).\n\n"
-        + emit("kCodewords36h11", 6, t36) + "\n\n" + emit("kCodewords16h5", 4, t16) + "\n")
+        "// BSD 2-Clause license (third_party/APRILTAG_LICENSE.md).\n"
+        "#pragma once\n\n"
+        + emit("BD_CODEWORDS_36H11", 6, t36) + "\n\n" + emit("BD_CODEWORDS_16H5", 4, t16) + "\n")
     print(f"wrote {out} ({len(t36)} + {len(t16)} codes)")
 
 

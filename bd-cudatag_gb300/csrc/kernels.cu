@@ -1,0 +1,1531 @@
+// sm_103a kernels of the batched AprilTag pipeline.
+//
+// One launch per stage covers every frame of a batch (see pipeline.cuh).
+// Stage map, with the reference kernels each one replaces
+// (detector/src/gpu_detector.cu):
+//   k_stats          tile min/max/mean, span+mean histograms, active extents,
+//                    and (last CTA of a frame) noise floor + Otsu + ROI rows
+//                    <- k_tile_stats :104, k_tile_histograms :140,
+//                       k_tile_reference :174, k_build_row_roi :282
+//   k_binarize_runs  3x3 pooled threshold, bit-packed binarization of the
+//                    row band, run extraction  <- k_tile_threshold :237,
+//                       k_binarize :362, k_find_runs :427
+//   k_merge          8-connected union-find of runs  <- k_merge_runs :509
+//   k_region_stats   area / bbox per root  <- k_region_stats :562
+//   k_cand_count     root flattening, tag-like filter, ordered per-band
+//                    bin ranks, (last CTA) bin bases <- k_collect_candidates :591
+//   k_cand_emit      ordered flattening into candidates  <- k_order_candidates :642
+//   k_fit            hull, four corners, per-family edge refinement
+//                    <- k_fit_quads :1081
+//   k_decode         8 variants per candidate, warp per variant
+//                    <- k_decode_quads :1438
+//   k_finalize       de-duplication, sort by id, FP64 homography
+//                    <- k_finalize :1542, host fill_homography :1739
+//
+// All FP32 arithmetic follows the reference expressions term by term and is
+// compiled with -fmad=false; transcendentals come from detmath.h.  With the
+// oracle built the same way, corners and margins match it bit for bit.
+
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <climits>
+#include <cstdint>
+
+#include "detmath.h"
+#include "families_data.inc"
+#include "pipeline.cuh"
+
+namespace bdgb {
+namespace {
+
+__device__ const uint64_t d_codes36h11[BD_CODEWORDS_36H11_COUNT] = {BD_CODEWORDS_36H11};
+__device__ const uint64_t d_codes16h5[BD_CODEWORDS_16H5_COUNT] = {BD_CODEWORDS_16H5};
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int family_dim(int fam) { return fam == 0 ? 8 : 6; }
+
+__device__ __forceinline__ int frame_of_band(const BatchDesc* __restrict__ b, int band) {
+    int lo = 0, hi = b->frames - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b->band_prefix[mid] <= band) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    return (1u << (threadIdx.x & 31)) - 1u;
+}
+
+// 4 bits, bit k = (byte k of `pixels` > t).
+__device__ __forceinline__ uint32_t white_bits4(uint32_t pixels, uint32_t t4) {
+    const uint32_t gt = __vcmpgtu4(pixels, t4);  // 0xff per byte where pixel > t
+    return (((gt >> 7) & 0x01010101u) * 0x10204080u) >> 28;
+}
+
+// ---------------------------------------------------------------------------
+// Union-find with the reference's invariant: a label only ever moves to a
+// smaller slot id, so the root of a component is its smallest run slot
+// (gpu_detector.cu:398-421).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
+    for (;;) {
+        const uint32_t p = parent[x];
+        if (p == x) return x;
+        const uint32_t gp = parent[p];
+        parent[x] = gp;
+        x = gp;
+    }
+}
+
+__device__ __forceinline__ uint32_t uf_root_readonly(const uint32_t* parent, uint32_t x) {
+    for (;;) {
+        const uint32_t p = __ldcg(parent + x);
+        if (p == x) return x;
+        x = p;
+    }
+}
+
+__device__ __forceinline__ void uf_union(uint32_t* parent, uint32_t a, uint32_t b) {
+    a = uf_find(parent, a);
+    b = uf_find(parent, b);
+    while (a != b) {
+        if (a > b) {
+            const uint32_t t = a;
+            a = b;
+            b = t;
+        }
+        const uint32_t old = atomicMin(&parent[b], a);
+        if (old == a) break;
+        b = uf_find(parent, old);
+    }
+}
+
+// ===========================================================================
+// 1. Tile statistics, histograms, active extents; the last CTA of a frame
+//    computes the frame references and the ROI row count.
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
+                                               const FrameIO* __restrict__ io) {
+    __shared__ uint32_t s_span[256];
+    __shared__ uint32_t s_mean[64];
+    __shared__ int s_lo, s_hi, s_last;
+    __shared__ float s_wb[64], s_sb[64], s_tot[2];
+    __shared__ float s_best_val[2];
+    __shared__ int s_best_idx[2];
+
+    const int tid = threadIdx.x;
+    const int fi = frame_of_band(b, blockIdx.x);
+    const FrameDesc& d = b->f[fi];
+    const int ty = blockIdx.x - b->band_prefix[fi];
+    FrameState* st = d.state;
+
+    s_span[tid] = 0;
+    if (tid < 64) s_mean[tid] = 0;
+    if (tid == 0) {
+        s_lo = INT_MAX;
+        s_hi = -1;
+    }
+    __syncthreads();
+
+    const uint8_t* gray = io[fi].gray;
+    const int64_t stride = io[fi].stride;
+    const int W = d.width, H = d.height, tw = d.tile_w;
+    const int y0 = ty * kTile;
+    const int rows = min(kTile, H - y0);
+    const bool vec = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 7u) == 0;
+    int lo = INT_MAX, hi = -1;
+    for (int tx = tid; tx < tw; tx += blockDim.x) {
+        const int x0 = tx * kTile;
+        const int cols = min(kTile, W - x0);
+        const uint8_t* p = gray + static_cast<int64_t>(y0) * stride + x0;
+        uint32_t mn, mx, sum = 0;
+        if (vec && cols == kTile) {
+            uint32_t vmin = 0xffffffffu, vmax = 0u;
+            for (int r = 0; r < rows; ++r) {
+                const uint2 v = *reinterpret_cast<const uint2*>(p + r * stride);
+                vmin = __vminu4(vmin, __vminu4(v.x, v.y));
+                vmax = __vmaxu4(vmax, __vmaxu4(v.x, v.y));
+                sum = __dp4a(v.x, 0x01010101u, sum);
+                sum = __dp4a(v.y, 0x01010101u, sum);
+            }
+            mn = min(min(vmin & 0xffu, (vmin >> 8) & 0xffu), min((vmin >> 16) & 0xffu, vmin >> 24));
+            mx = max(max(vmax & 0xffu, (vmax >> 8) & 0xffu), max((vmax >> 16) & 0xffu, vmax >> 24));
+        } else {
+            mn = 255u;
+            mx = 0u;
+            for (int r = 0; r < rows; ++r) {
+                for (int c = 0; c < cols; ++c) {
+                    const uint32_t v = p[r * stride + c];
+                    mn = min(mn, v);
+                    mx = max(mx, v);
+                    sum += v;
+                }
+            }
+        }
+        const uint32_t count = static_cast<uint32_t>(rows * cols);
+        const uint32_t mean = (sum + count / 2) / count;
+        const int idx = ty * tw + tx;
+        d.tile_min[idx] = static_cast<uint8_t>(mn);
+        d.tile_max[idx] = static_cast<uint8_t>(mx);
+        atomicAdd(&s_span[(mx - mn) & 0xffu], 1u);
+        atomicAdd(&s_mean[mean >> 2], 1u);
+        if (static_cast<int>(mx - mn) >= kMinTileContrast) {
+            lo = min(lo, tx);
+            hi = max(hi, tx);
+        }
+    }
+    lo = __reduce_min_sync(kFull, lo);
+    hi = __reduce_max_sync(kFull, hi);
+    if ((tid & 31) == 0 && hi >= 0) {
+        atomicMin(&s_lo, lo);
+        atomicMax(&s_hi, hi);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        d.row_lo[ty] = s_hi >= 0 ? s_lo : -1;
+        d.row_hi[ty] = s_hi;
+        if (s_hi >= 0) {
+            atomicMax(&st->top_enc, static_cast<uint32_t>(d.tile_h - ty));
+            atomicMax(&st->bottom_enc, static_cast<uint32_t>(ty + 1));
+        }
+    }
+    if (s_span[tid]) atomicAdd(&st->span_hist[tid], s_span[tid]);
+    if (tid < 64 && s_mean[tid]) atomicAdd(&st->mean_hist[tid], s_mean[tid]);
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&st->done_stats, 1u) == static_cast<uint32_t>(d.tile_h - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+
+    // --- frame references (reference k_tile_reference :174-230) ---
+    const int lane = tid & 31;
+    if (tid < 32) {
+        // Lower quartile of the span histogram: first bin whose cumulative
+        // count exceeds total / 4.
+        uint32_t v[8];
+        uint32_t local = 0;
+        for (int k = 0; k < 8; ++k) {
+            v[k] = __ldcg(&st->span_hist[lane * 8 + k]);
+            local += v[k];
+        }
+        uint32_t incl = local;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t n = __shfl_up_sync(kFull, incl, off);
+            if (lane >= off) incl += n;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        uint32_t span = 0;
+        if (total > 0) {
+            const uint32_t target = total / 4;
+            uint32_t seen = incl - local;
+            int hit = -1;
+            for (int k = 0; k < 8; ++k) {
+                seen += v[k];
+                if (hit < 0 && seen > target) hit = lane * 8 + k;
+            }
+            const unsigned any = __ballot_sync(kFull, hit >= 0);
+            span = static_cast<uint32_t>(__shfl_sync(kFull, hit, __ffs(any) - 1));
+        }
+        if (lane == 0) st->ref[0] = span;
+    } else if (tid == 32) {
+        // Otsu prefix sums, sequential so every float sum is rounded in the
+        // reference's order.
+        float total = 0.0f, sum = 0.0f;
+        for (int i = 0; i < 64; ++i) {
+            const float m = static_cast<float>(__ldcg(&st->mean_hist[i]));
+            total += m;
+            sum += static_cast<float>(i) * m;
+            s_wb[i] = total;
+            s_sb[i] = sum;
+        }
+        s_tot[0] = total;
+        s_tot[1] = sum;
+    }
+    __syncthreads();
+    if (tid < 64) {
+        // Between-class variance of every split; first maximum wins.
+        const float total = s_tot[0], sum = s_tot[1];
+        const float wb = s_wb[tid];
+        const float wa = total - wb;
+        float between = -2.0f;
+        if (total > 0.0f && wb > 0.0f && wa > 0.0f) {
+            const float sb = s_sb[tid];
+            const float mean_below = sb / wb;
+            const float mean_above = (sum - sb) / wa;
+            const float delta = mean_below - mean_above;
+            between = wb * wa * delta * delta;
+        }
+        int idx = tid;
+        for (int off = 16; off > 0; off >>= 1) {
+            const float ov = __shfl_down_sync(kFull, between, off);
+            const int oi = __shfl_down_sync(kFull, idx, off);
+            if (ov > between || (ov == between && oi < idx)) {
+                between = ov;
+                idx = oi;
+            }
+        }
+        if (lane == 0) {
+            s_best_val[tid >> 5] = between;
+            s_best_idx[tid >> 5] = idx;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float best = s_best_val[0];
+        int idx = s_best_idx[0];
+        if (s_best_val[1] > best) {
+            best = s_best_val[1];
+            idx = s_best_idx[1];
+        }
+        const int otsu = best > -1.0f ? idx : 0;
+        st->ref[1] = static_cast<uint32_t>(otsu * 4 + 2);
+        // ROI tile rows: every row between the first and last contrasting
+        // tile row, one row of halo each side (reference :314-330, :2117).
+        const uint32_t te = __ldcg(&st->top_enc), be = __ldcg(&st->bottom_enc);
+        uint32_t roi = 0;
+        if (be > 0) {
+            const int top = d.tile_h - static_cast<int>(te);
+            const int bottom = static_cast<int>(be) - 1;
+            roi = static_cast<uint32_t>(min(bottom + 1, d.tile_h - 1) - max(top - 1, 0) + 1);
+        }
+        st->counts[4] = roi;
+    }
+}
+
+// ===========================================================================
+// 2. Pooled threshold, binarization of the row band and run extraction for
+//    one band of 8 rows; warp w owns row y0 + w.
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restrict__ b,
+                                                       const FrameIO* __restrict__ io) {
+    __shared__ uint8_t s_thresh[BD_MAX_WIDTH / kTile];
+    __shared__ uint32_t s_bits[kTile][BD_MAX_WIDTH / 32];
+    __shared__ uint32_t s_runs;
+
+    const int tid = threadIdx.x;
+    const int fi = frame_of_band(b, blockIdx.x);
+    const FrameDesc& d = b->f[fi];
+    const int ty = blockIdx.x - b->band_prefix[fi];
+    FrameState* st = d.state;
+    const int W = d.width, H = d.height, tw = d.tile_w, th = d.tile_h, words = d.words;
+    const int y0 = ty * kTile;
+    const int rows = min(kTile, H - y0);
+
+    const int top = th - static_cast<int>(st->top_enc);
+    const int bottom = static_cast<int>(st->bottom_enc) - 1;
+    const bool on = bottom >= 0 && ty >= top - 1 && ty <= bottom + 1;
+    if (!on) {
+        for (int i = tid; i < rows * words; i += blockDim.x) {
+            d.bits[static_cast<int64_t>(y0 + i / words) * words + i % words] = 0xffffffffu;
+        }
+        if (tid < rows) d.row_count[y0 + tid] = 0;
+        return;
+    }
+    if (tid == 0) s_runs = 0;
+
+    // Row band: contrasting tiles +- 4, or the whole row (reference :345-355).
+    const int lo = d.row_lo[ty], hi = d.row_hi[ty];
+    const int start = lo < 0 ? 0 : max(0, lo - 4);
+    const int end = lo < 0 ? tw - 1 : min(tw - 1, hi + 4);
+    const int wx_lo = start >> 2;
+    const int wx_hi = end >> 2;
+
+    // Pooled thresholds (reference k_tile_threshold :237-270).
+    const uint32_t ref0 = st->ref[0], ref1 = st->ref[1];
+    const int floor_contrast = max(kMinTileContrast, static_cast<int>((ref0 * 3) / 2));
+    const int t_end = min(4 * wx_hi + 3, tw - 1);
+    for (int t = 4 * wx_lo + tid; t <= t_end; t += blockDim.x) {
+        int mn = 255, mx = 0;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int yy = ty + dy;
+            if (yy < 0 || yy >= th) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int xx = t + dx;
+                if (xx < 0 || xx >= tw) continue;
+                mn = min(mn, static_cast<int>(d.tile_min[yy * tw + xx]));
+                mx = max(mx, static_cast<int>(d.tile_max[yy * tw + xx]));
+            }
+        }
+        int thr = static_cast<int>(ref1);
+        if (mx - mn >= floor_contrast) thr = (mn + mx + 1) >> 1;
+        s_thresh[t] = static_cast<uint8_t>(thr);
+    }
+    __syncthreads();
+
+    const int w = tid >> 5, lane = tid & 31;
+    const uint8_t* gray = io[fi].gray;
+    const int64_t stride = io[fi].stride;
+    const bool vec = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 15u) == 0;
+    if (w < rows) {
+        const int y = y0 + w;
+        const uint8_t* row = gray + static_cast<int64_t>(y) * stride;
+        for (int wx = lane; wx < words; wx += 32) {
+            uint32_t m = 0xffffffffu;
+            if (wx >= wx_lo && wx <= wx_hi) {
+                const int x = wx << 5;
+                if (vec && x + 32 <= W) {
+                    const uint4 a = *reinterpret_cast<const uint4*>(row + x);
+                    const uint4 c = *reinterpret_cast<const uint4*>(row + x + 16);
+                    const int t0 = x >> 3;
+                    const uint32_t q0 = s_thresh[t0] * 0x01010101u, q1 = s_thresh[t0 + 1] * 0x01010101u;
+                    const uint32_t q2 = s_thresh[t0 + 2] * 0x01010101u, q3 = s_thresh[t0 + 3] * 0x01010101u;
+                    m = white_bits4(a.x, q0) | (white_bits4(a.y, q0) << 4) |
+                        (white_bits4(a.z, q1) << 8) | (white_bits4(a.w, q1) << 12) |
+                        (white_bits4(c.x, q2) << 16) | (white_bits4(c.y, q2) << 20) |
+                        (white_bits4(c.z, q3) << 24) | (white_bits4(c.w, q3) << 28);
+                } else {
+                    m = 0u;
+                    for (int k = 0; k < 32; ++k) {
+                        const int xx = x + k;
+                        const bool white = xx >= W || row[xx] > s_thresh[xx >> 3];
+                        m |= (white ? 1u : 0u) << k;
+                    }
+                }
+            }
+            d.bits[static_cast<int64_t>(y) * words + wx] = m;
+            s_bits[w][wx] = m;
+        }
+        __syncwarp();
+
+        // Runs of black pixels; a run restarts at every 32-pixel word and
+        // k_merge rejoins the pieces (reference k_find_runs :427-504).
+        const int per = (words + 31) >> 5;
+        const int c0 = lane * per;
+        const int c1 = min(c0 + per, words);
+        uint32_t cnt = 0;
+        for (int c = c0; c < c1; ++c) {
+            const uint32_t m = s_bits[w][c];
+            cnt += __popc(~m & ((m << 1) | 1u));
+        }
+        uint32_t incl = cnt;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t n = __shfl_up_sync(kFull, incl, off);
+            if (lane >= off) incl += n;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        const uint32_t row_cap = static_cast<uint32_t>(d.row_cap);
+        uint32_t index = incl - cnt;
+        const uint32_t slot_base = static_cast<uint32_t>(y) * row_cap;
+        for (int c = c0; c < c1; ++c) {
+            const uint32_t m = s_bits[w][c];
+            uint32_t starts = ~m & ((m << 1) | 1u);
+            const int last = min(31, W - 1 - (c << 5));
+            while (starts) {
+                const int s = __ffs(starts) - 1;
+                starts &= starts - 1u;
+                const int x0 = (c << 5) + s;
+                if (x0 < W && index < row_cap) {
+                    const int next_white = __ffs(m >> s);
+                    int e = next_white ? (s + next_white - 2) : last;
+                    e = min(e, last);
+                    const int x1 = (c << 5) + e;
+                    const uint32_t id = slot_base + index;
+                    d.runs[id] = (static_cast<uint32_t>(x0) & 0xffffu) | (static_cast<uint32_t>(x1) << 16);
+                    d.parent[id] = id;
+                    d.area[id] = 0;
+                    reinterpret_cast<uint4*>(d.bbox)[id] = make_uint4(kNone, kNone, 0u, 0u);
+                }
+                ++index;
+            }
+        }
+        if (lane == 0) {
+            const uint32_t kept = min(total, row_cap);
+            d.row_count[y] = kept;
+            atomicAdd(&s_runs, kept);
+        }
+    }
+    __syncthreads();
+    if (tid == 0 && s_runs) atomicAdd(&st->counts[2], s_runs);
+}
+
+// ===========================================================================
+// 3. Union of same-row fragments and 8-connected runs of the row above
+//    (reference k_merge_runs :509-557).
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b) {
+    const int fi = frame_of_band(b, blockIdx.x);
+    const FrameDesc& d = b->f[fi];
+    const int ty = blockIdx.x - b->band_prefix[fi];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y = ty * kTile + w;
+    if (y <= 0 || y >= d.height) return;
+    const int n = static_cast<int>(d.row_count[y]);
+    if (n == 0) return;
+    const int row_cap = d.row_cap;
+    const int prev_n = static_cast<int>(d.row_count[y - 1]);
+    const uint32_t* cur = d.runs + static_cast<int64_t>(y) * row_cap;
+    const uint32_t* prev = d.runs + static_cast<int64_t>(y - 1) * row_cap;
+    const uint32_t cur_base = static_cast<uint32_t>(y * row_cap);
+    const uint32_t prev_base = static_cast<uint32_t>((y - 1) * row_cap);
+    uint32_t* parent = d.parent;
+    for (int i = lane; i < n; i += 32) {
+        const uint32_t run = cur[i];
+        const int x0 = static_cast<int>(run & 0xffffu);
+        const int x1 = static_cast<int>(run >> 16);
+        if (i > 0) {
+            const int px1 = static_cast<int>(cur[i - 1] >> 16);
+            if (px1 + 1 >= x0) uf_union(parent, cur_base + i, cur_base + i - 1);
+        }
+        if (prev_n == 0) continue;
+        int lo = 0, hi = prev_n - 1, first = prev_n;
+        while (lo <= hi) {
+            const int mid = (lo + hi) >> 1;
+            if (static_cast<int>(prev[mid] >> 16) >= x0 - 1) {
+                first = mid;
+                hi = mid - 1;
+            } else {
+                lo = mid + 1;
+            }
+        }
+        for (int k = first; k < prev_n; ++k) {
+            const int px0 = static_cast<int>(prev[k] & 0xffffu);
+            if (px0 > x1 + 1) break;
+            uf_union(parent, cur_base + i, prev_base + k);
+        }
+    }
+}
+
+// ===========================================================================
+// 4. Area and bounding box per root (reference k_region_stats :562-586).
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_region_stats(const BatchDesc* __restrict__ b) {
+    const int fi = frame_of_band(b, blockIdx.x);
+    const FrameDesc& d = b->f[fi];
+    const int ty = blockIdx.x - b->band_prefix[fi];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y = ty * kTile + w;
+    if (y >= d.height) return;
+    const int n = static_cast<int>(d.row_count[y]);
+    const uint32_t base = static_cast<uint32_t>(y * d.row_cap);
+    for (int i = lane; i < n; i += 32) {
+        const uint32_t idx = base + static_cast<uint32_t>(i);
+        const uint32_t root = uf_find(d.parent, idx);
+        const uint32_t run = d.runs[idx];
+        const uint32_t x0 = run & 0xffffu, x1 = run >> 16;
+        atomicAdd(&d.area[root], x1 - x0 + 1);
+        atomicMin(&d.bbox[root * 4 + 0], x0);
+        atomicMin(&d.bbox[root * 4 + 1], static_cast<uint32_t>(y));
+        atomicMax(&d.bbox[root * 4 + 2], x1);
+        atomicMax(&d.bbox[root * 4 + 3], static_cast<uint32_t>(y));
+    }
+}
+
+// ===========================================================================
+// 5. Root labels, the tag-like filter and ordered ranks.  A candidate's
+//    flattened position is (area bin, band, row, slot) order, which is
+//    ascending root id inside a bin; the reference orders a bin by atomicAdd
+//    arrival (k_collect_candidates :591-638).
+// ===========================================================================
+__device__ __forceinline__ int candidate_bin(const FrameDesc& d, uint32_t idx) {
+    const int a = static_cast<int>(d.area[idx]);
+    if (a < d.min_cluster_pixels) return -1;
+    const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[idx];
+    const int x0 = static_cast<int>(bb.x), y0 = static_cast<int>(bb.y);
+    const int x1 = static_cast<int>(bb.z), y1 = static_cast<int>(bb.w);
+    const int bw = x1 - x0 + 1;
+    const int bh = y1 - y0 + 1;
+    if (bw < d.min_tag_pixels || bh < d.min_tag_pixels) return -1;
+    if (x0 <= 0 || y0 <= 0 || x1 >= d.width - 1 || y1 >= d.height - 1) return -1;
+    if (bw > 6 * bh || bh > 6 * bw) return -1;
+    const float fill = static_cast<float>(a) / static_cast<float>(bw * bh);
+    if (fill < 0.18f || fill > 0.95f) return -1;
+    const int log2_area = 31 - __clz(static_cast<uint32_t>(a));
+    return 63 - min(log2_area, 63);
+}
+
+__global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict__ b) {
+    __shared__ uint32_t s_rowbin[kTile][64];
+    __shared__ uint32_t s_chunk[32][64];
+    __shared__ uint32_t s_total[64];
+    __shared__ int s_last;
+
+    const int tid = threadIdx.x;
+    const int fi = frame_of_band(b, blockIdx.x);
+    const FrameDesc& d = b->f[fi];
+    const int ty = blockIdx.x - b->band_prefix[fi];
+    FrameState* st = d.state;
+    for (int i = tid; i < kTile * 64; i += blockDim.x) (&s_rowbin[0][0])[i] = 0;
+    __syncthreads();
+
+    const int w = tid >> 5, lane = tid & 31;
+    const int y = ty * kTile + w;
+    const int n = y < d.height ? static_cast<int>(d.row_count[y]) : 0;
+    const uint32_t base = static_cast<uint32_t>(y * d.row_cap);
+    for (int c = 0; c < n; c += 32) {
+        const int i = c + lane;
+        int bin = -1;
+        uint32_t idx = 0;
+        if (i < n) {
+            idx = base + static_cast<uint32_t>(i);
+            const uint32_t root = uf_root_readonly(d.parent, idx);
+            d.parent[idx] = root;
+            if (root == idx) bin = candidate_bin(d, idx);
+        }
+        const uint32_t key = bin >= 0 ? static_cast<uint32_t>(bin) : 64u + lane;
+        const uint32_t peers = __match_any_sync(kFull, key);
+        uint32_t meta = kNone;
+        uint32_t rank = 0;
+        if (bin >= 0) {
+            rank = __popc(peers & lanemask_lt());
+            meta = (static_cast<uint32_t>(bin) << 24) | (s_rowbin[w][bin] + rank);
+        }
+        __syncwarp();
+        if (bin >= 0 && rank == 0) s_rowbin[w][bin] += __popc(peers);
+        __syncwarp();
+        if (i < n) d.cand_meta[idx] = meta;
+    }
+    __syncthreads();
+    // Exclusive prefix over the band's rows per bin; band totals.
+    if (tid < 64) {
+        uint32_t run = 0;
+        for (int r = 0; r < kTile; ++r) {
+            const uint32_t v = s_rowbin[r][tid];
+            s_rowbin[r][tid] = run;
+            run += v;
+        }
+        d.band_bins[ty * 64 + tid] = run;
+    }
+    __syncthreads();
+    for (int c = 0; c < n; c += 32) {
+        const int i = c + lane;
+        if (i < n) {
+            const uint32_t idx = base + static_cast<uint32_t>(i);
+            const uint32_t meta = d.cand_meta[idx];
+            if (meta != kNone) d.cand_meta[idx] = meta + s_rowbin[w][meta >> 24];
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&st->done_cands, 1u) == static_cast<uint32_t>(d.tile_h - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+
+    // Last band: exclusive prefix of every bin over the bands (in place),
+    // 32 bands at a time through shared memory.
+    const int th = d.tile_h;
+    uint32_t carry = 0;  // per bin, owned by thread tid < 64
+    for (int band0 = 0; band0 < th; band0 += 32) {
+        const int nb = min(32, th - band0);
+        for (int k = tid; k < nb * 64; k += blockDim.x) {
+            s_chunk[k >> 6][k & 63] = __ldcg(&d.band_bins[(band0 + (k >> 6)) * 64 + (k & 63)]);
+        }
+        __syncthreads();
+        if (tid < 64) {
+            for (int r = 0; r < nb; ++r) {
+                const uint32_t v = s_chunk[r][tid];
+                s_chunk[r][tid] = carry;
+                carry += v;
+            }
+        }
+        __syncthreads();
+        for (int k = tid; k < nb * 64; k += blockDim.x) {
+            d.band_bins[(band0 + (k >> 6)) * 64 + (k & 63)] = s_chunk[k >> 6][k & 63];
+        }
+        __syncthreads();
+    }
+    if (tid < 64) s_total[tid] = carry;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t pos = 0;
+        for (int bin = 0; bin < 64; ++bin) {
+            st->bin_base[bin] = pos;
+            pos += s_total[bin];
+        }
+        st->counts[0] = pos;
+        st->n_candidates = min(pos, static_cast<uint32_t>(d.max_candidates));
+    }
+}
+
+// ===========================================================================
+// 6. Ordered flattening (reference k_order_candidates :642-654).
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_cand_emit(const BatchDesc* __restrict__ b) {
+    const int fi = frame_of_band(b, blockIdx.x);
+    const FrameDesc& d = b->f[fi];
+    const int ty = blockIdx.x - b->band_prefix[fi];
+    const FrameState* st = d.state;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y = ty * kTile + w;
+    if (y >= d.height) return;
+    const int n = static_cast<int>(d.row_count[y]);
+    const uint32_t limit = st->n_candidates;
+    const uint32_t base = static_cast<uint32_t>(y * d.row_cap);
+    for (int i = lane; i < n; i += 32) {
+        const uint32_t idx = base + static_cast<uint32_t>(i);
+        const uint32_t meta = d.cand_meta[idx];
+        if (meta == kNone) continue;
+        const uint32_t bin = meta >> 24;
+        const uint32_t pos = st->bin_base[bin] + d.band_bins[ty * 64 + bin] + (meta & 0xffffffu);
+        if (pos < limit) d.candidates[pos] = idx;
+    }
+}
+
+// ===========================================================================
+// 7. Quad fit (reference k_fit_quads :1081-1241 and helpers :659-1076).
+// ===========================================================================
+__device__ __forceinline__ uint32_t pack_point(int x, int y) {
+    return (static_cast<uint32_t>(x) & 0xffffu) | (static_cast<uint32_t>(y) << 16);
+}
+
+__device__ bool hull_to_quad(const uint32_t* hull, int count, float quad[4][2]) {
+    if (count < 4 || count > kMaxHullVertices) return false;
+    float vx[kFitDirections];
+    float vy[kFitDirections];
+    if (count > kFitDirections) return false;
+    for (int i = 0; i < count; ++i) {
+        vx[i] = static_cast<float>(hull[i] & 0xffffu);
+        vy[i] = static_cast<float>(hull[i] >> 16);
+    }
+    while (count > 4) {
+        int best = -1;
+        float best_area = FLT_MAX;
+        for (int i = 0; i < count; ++i) {
+            const int prev = (i + count - 1) % count;
+            const int next = (i + 1) % count;
+            const float ax = vx[i] - vx[prev];
+            const float ay = vy[i] - vy[prev];
+            const float bx = vx[next] - vx[i];
+            const float by = vy[next] - vy[i];
+            const float area = fabsf(ax * by - ay * bx) * 0.5f;
+            if (area < best_area) {
+                best_area = area;
+                best = i;
+            }
+        }
+        if (best < 0) return false;
+        for (int i = best; i + 1 < count; ++i) {
+            vx[i] = vx[i + 1];
+            vy[i] = vy[i + 1];
+        }
+        --count;
+    }
+    float area2 = 0.0f;
+    for (int i = 0; i < 4; ++i) {
+        const int j = (i + 1) & 3;
+        area2 += vx[i] * vy[j] - vx[j] * vy[i];
+    }
+    if (fabsf(area2) < 24.0f) return false;
+    if (area2 < 0.0f) {
+        for (int i = 0; i < 2; ++i) {
+            const float tx = vx[i + 1], ty = vy[i + 1];
+            vx[i + 1] = vx[3 - i];
+            vy[i + 1] = vy[3 - i];
+            vx[3 - i] = tx;
+            vy[3 - i] = ty;
+        }
+    }
+    float min_side = FLT_MAX, max_side = 0.0f;
+    for (int i = 0; i < 4; ++i) {
+        const int j = (i + 1) & 3;
+        const float ex = vx[j] - vx[i];
+        const float ey = vy[j] - vy[i];
+        const float len = sqrtf(ex * ex + ey * ey);
+        if (len < 4.0f) return false;
+        min_side = fminf(min_side, len);
+        max_side = fmaxf(max_side, len);
+        const int p = (i + 3) & 3;
+        const float ax = vx[i] - vx[p];
+        const float ay = vy[i] - vy[p];
+        const float bx = vx[j] - vx[i];
+        const float by = vy[j] - vy[i];
+        if (ax * by - ay * bx <= 0.0f) return false;
+        const float dot = ax * bx + ay * by;
+        const float n1 = sqrtf(ax * ax + ay * ay);
+        const float n2 = sqrtf(bx * bx + by * by);
+        if (n1 < 1e-3f || n2 < 1e-3f) return false;
+        if (fabsf(dot / (n1 * n2)) > 0.97f) return false;
+    }
+    if (max_side > 12.0f * min_side) return false;
+    const float cx = 0.25f * (vx[0] + vx[1] + vx[2] + vx[3]);
+    const float cy = 0.25f * (vy[0] + vy[1] + vy[2] + vy[3]);
+    for (int i = 0; i < 4; ++i) {
+        const float dx = vx[i] - cx;
+        const float dy = vy[i] - cy;
+        const float len = sqrtf(dx * dx + dy * dy);
+        if (len > 1e-3f) {
+            vx[i] += dx / len * 0.65f;
+            vy[i] += dy / len * 0.65f;
+        }
+    }
+    for (int i = 0; i < 4; ++i) {
+        quad[i][0] = vx[i];
+        quad[i][1] = vy[i];
+    }
+    return true;
+}
+
+__device__ __forceinline__ float sample_bilinear(const uint8_t* image, int width, int height,
+                                                 int64_t stride, float x, float y) {
+    if (!(x >= 0.0f && y >= 0.0f && x < static_cast<float>(width - 1) &&
+          y < static_cast<float>(height - 1))) {
+        return -1.0f;
+    }
+    const int ix = static_cast<int>(x);
+    const int iy = static_cast<int>(y);
+    const float fx = x - static_cast<float>(ix);
+    const float fy = y - static_cast<float>(iy);
+    const uint8_t* p = image + static_cast<int64_t>(iy) * stride + ix;
+    const float a = p[0];
+    const float bb = p[1];
+    const float c = p[stride];
+    const float dd = p[stride + 1];
+    return (a * (1.0f - fx) + bb * fx) * (1.0f - fy) + (c * (1.0f - fx) + dd * fx) * fy;
+}
+
+__device__ __forceinline__ bool intersect_lines(const float li[4], const float lj[4], float* x,
+                                                float* y) {
+    const float det = li[2] * lj[3] - li[3] * lj[2];
+    if (fabsf(det) < 0.2f) return false;
+    const float di = li[2] * li[0] + li[3] * li[1];
+    const float dj = lj[2] * lj[0] + lj[3] * lj[1];
+    *x = (di * lj[3] - li[3] * dj) / det;
+    *y = (li[2] * dj - di * lj[2]) / det;
+    return true;
+}
+
+__device__ __forceinline__ float directional_rise(const uint8_t* image, int width, int height,
+                                                  int64_t stride, float x, float y, float dx,
+                                                  float dy) {
+    const float ahead = sample_bilinear(image, width, height, stride, x + dx * 0.7f, y + dy * 0.7f);
+    const float behind = sample_bilinear(image, width, height, stride, x - dx * 0.7f, y - dy * 0.7f);
+    if (ahead < 0.0f || behind < 0.0f) return 0.0f;
+    return ahead - behind;
+}
+
+// One warp fits one edge: lanes < samples probe across the edge, moments
+// are reduced with the shuffle tree, lane 0 turns them into a line
+// (reference fit_edge_line_warp :881-1016).
+__device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8_t* image, int width,
+                                   int height, int64_t stride, int dim, bool first_pass, int lane,
+                                   float line[4]) {
+    const int bi = (edge + 1) & 3;
+    const float ax = quad[edge][0], ay = quad[edge][1];
+    const float bx = quad[bi][0], by = quad[bi][1];
+    const float ex = bx - ax;
+    const float ey = by - ay;
+    const float len = sqrtf(ex * ex + ey * ey);
+    if (len < 8.0f) return false;
+    const float nx = ey / len;
+    const float ny = -ex / len;
+    const float cell = len / static_cast<float>(dim);
+    const float range = first_pass ? fminf(fmaxf(1.15f * cell, 1.5f), 2.5f * cell)
+                                   : fminf(fmaxf(0.30f * cell, 0.8f), 2.0f);
+    const int half = min(max(2, static_cast<int>(ceilf(range / 0.75f))), kFitProbeHalf);
+    const int probes = 2 * half + 1;
+    const float step = range / static_cast<float>(half);
+    const int samples = min(max(static_cast<int>(len / 6.0f), 8), 16);
+
+    float mx = 0.0f, my = 0.0f, mxx = 0.0f, mxy = 0.0f, myy = 0.0f;
+    int used = 0;
+    if (lane < samples) {
+        const float alpha = static_cast<float>(lane + 1) / static_cast<float>(samples + 1);
+        const float px = ax + alpha * ex;
+        const float py = ay + alpha * ey;
+        float mags[kFitProbeHalf * 2 + 1];
+        float best_mag = 0.0f;
+        int best = -1;
+        for (int i = 0; i < probes; ++i) {
+            const float t = step * static_cast<float>(i - half);
+            const float mag = directional_rise(image, width, height, stride, px + nx * t,
+                                               py + ny * t, nx, ny);
+            mags[i] = mag;
+            if (mag > best_mag) {
+                best_mag = mag;
+                best = i;
+            }
+        }
+        if (first_pass && best > 2) {
+            const float accept = 0.70f * best_mag;
+            for (int i = 1; i + 1 < best; ++i) {
+                if (mags[i] < accept || mags[i] < mags[i - 1] || mags[i] < mags[i + 1]) continue;
+                float valley = FLT_MAX;
+                for (int k = i + 1; k < best; ++k) valley = fminf(valley, mags[k]);
+                if (valley < 0.5f * mags[i]) {
+                    best = i;
+                    best_mag = mags[i];
+                    break;
+                }
+            }
+        }
+        if (best >= 0 && best_mag >= 6.0f) {
+            float t = step * static_cast<float>(best - half);
+            if (best > 0 && best < probes - 1) {
+                const float m0 = directional_rise(image, width, height, stride, px + nx * (t - step),
+                                                  py + ny * (t - step), nx, ny);
+                const float m2 = directional_rise(image, width, height, stride, px + nx * (t + step),
+                                                  py + ny * (t + step), nx, ny);
+                const float den = m0 - 2.0f * best_mag + m2;
+                if (den < -1e-3f) t += fminf(fmaxf(0.5f * (m0 - m2) / den, -0.5f), 0.5f) * step;
+            }
+            const float x = px + nx * t;
+            const float y = py + ny * t;
+            mx = x;
+            my = y;
+            mxx = x * x;
+            mxy = x * y;
+            myy = y * y;
+            used = 1;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        mx += __shfl_down_sync(kFull, mx, off);
+        my += __shfl_down_sync(kFull, my, off);
+        mxx += __shfl_down_sync(kFull, mxx, off);
+        mxy += __shfl_down_sync(kFull, mxy, off);
+        myy += __shfl_down_sync(kFull, myy, off);
+        used += __shfl_down_sync(kFull, used, off);
+    }
+    if (lane != 0) return true;
+    if (used < 4) return false;
+    const float inv = 1.0f / static_cast<float>(used);
+    const float cx = mx * inv;
+    const float cy = my * inv;
+    const float cxx = mxx * inv - cx * cx;
+    const float cxy = mxy * inv - cx * cy;
+    const float cyy = myy * inv - cy * cy;
+    const float theta = 0.5f * bdmath::atan2(2.0f * cxy, cxx - cyy);
+    float s, c;
+    bdmath::sincos(theta, &s, &c);
+    line[0] = cx;
+    line[1] = cy;
+    line[2] = -s;
+    line[3] = c;
+    return true;
+}
+
+__device__ float apply_refined_lines(float quad[4][2], const float lines[4][4], const int have[4]) {
+    int line_count = 0;
+    for (int i = 0; i < 4; ++i) line_count += have[i] ? 1 : 0;
+    if (line_count < 3) return 0.0f;
+    float refined[4][2];
+    for (int i = 0; i < 4; ++i) {
+        refined[i][0] = quad[i][0];
+        refined[i][1] = quad[i][1];
+    }
+    float extent = 0.0f;
+    for (int i = 0; i < 4; ++i) {
+        const int j = (i + 1) & 3;
+        extent = fmaxf(extent, bdmath::hypot(quad[j][0] - quad[i][0], quad[j][1] - quad[i][1]));
+    }
+    const float max_shift = fminf(fmaxf(0.15f * extent, 4.0f), 16.0f);
+    float moved = 0.0f;
+    for (int i = 0; i < 4; ++i) {
+        const int j = (i + 1) & 3;
+        if (!have[i] || !have[j]) continue;
+        float x, y;
+        if (!intersect_lines(lines[i], lines[j], &x, &y)) continue;
+        const int corner = j;
+        const float dx = x - quad[corner][0];
+        const float dy = y - quad[corner][1];
+        if (dx * dx + dy * dy > max_shift * max_shift) continue;
+        refined[corner][0] = x;
+        refined[corner][1] = y;
+        moved = fmaxf(moved, sqrtf(dx * dx + dy * dy));
+    }
+    for (int i = 0; i < 4; ++i) {
+        const int j = (i + 1) & 3;
+        if (bdmath::hypot(refined[j][0] - refined[i][0], refined[j][1] - refined[i][1]) < 3.0f) {
+            return 0.0f;
+        }
+    }
+    float area2 = 0.0f;
+    for (int i = 0; i < 4; ++i) {
+        const int j = (i + 1) & 3;
+        area2 += refined[i][0] * refined[j][1] - refined[j][0] * refined[i][1];
+    }
+    if (area2 <= 0.0f) return 0.0f;
+    for (int i = 0; i < 4; ++i) {
+        quad[i][0] = refined[i][0];
+        quad[i][1] = refined[i][1];
+    }
+    return moved;
+}
+
+constexpr int kFitThreads = 128;
+constexpr int kFitWarps = kFitThreads / 32;
+
+// Flattened (frame, candidate) work list: CTA c takes items c, c + grid, ...
+__global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict__ b,
+                                                     const FrameIO* __restrict__ io) {
+    __shared__ uint32_t boundary[2 * kMaxBoundaryRows];
+    __shared__ float probe_dot[kFitWarps][kFitDirections];
+    __shared__ uint32_t probe_point[kFitWarps][kFitDirections];
+    __shared__ uint32_t extreme[kFitDirections];
+    __shared__ float hull_quad[4][2];
+    __shared__ float fit_quad[4][2];
+    __shared__ float edge_lines[4][4];
+    __shared__ int edge_have[4];
+    __shared__ int quad_ok;
+    __shared__ float refine_moved;
+    __shared__ int s_prefix[kMaxFrames + 1];
+
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        int run = 0;
+        for (int f = 0; f < b->frames; ++f) {
+            s_prefix[f] = run;
+            run += static_cast<int>(b->f[f].state->n_candidates);
+        }
+        s_prefix[b->frames] = run;
+    }
+    __syncthreads();
+    const int total = s_prefix[b->frames];
+    const int dir = tid & 31;
+    const int part = tid >> 5;
+    float ux, uy;
+    {
+        const float angle =
+            6.28318530718f * static_cast<float>(dir) / static_cast<float>(kFitDirections);
+        bdmath::sincos(angle, &uy, &ux);
+    }
+
+    for (int item = blockIdx.x; item < total; item += gridDim.x) {
+        int fi = 0;
+        while (s_prefix[fi + 1] <= item) ++fi;
+        const FrameDesc& d = b->f[fi];
+        const int ci = item - s_prefix[fi];
+        const int mc = d.max_candidates;
+        const uint8_t* gray = io[fi].gray;
+        const int64_t stride = io[fi].stride;
+        const uint32_t root = d.candidates[ci];
+        const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[root];
+        const int x0 = static_cast<int>(bb.x), y0 = static_cast<int>(bb.y);
+        const int x1 = static_cast<int>(bb.z), y1 = static_cast<int>(bb.w);
+        const int rows = y1 - y0 + 1;
+        const int kept = min(rows, kMaxBoundaryRows);
+        const int points = 2 * kept;
+
+        // Leftmost / rightmost run of the component in each sampled row
+        // (reference collect_row_extremes :676-715).
+        for (int s = tid; s < kept; s += blockDim.x) {
+            const int y = y0 + (kept > 1 ? (s * (rows - 1)) / (kept - 1) : 0);
+            const int n = static_cast<int>(d.row_count[y]);
+            const uint32_t* row_runs = d.runs + static_cast<int64_t>(y) * d.row_cap;
+            int lo = 0, hi = n - 1, first = n;
+            while (lo <= hi) {
+                const int mid = (lo + hi) >> 1;
+                if (static_cast<int>(row_runs[mid] >> 16) >= x0) {
+                    first = mid;
+                    hi = mid - 1;
+                } else {
+                    lo = mid + 1;
+                }
+            }
+            const uint32_t base = static_cast<uint32_t>(y * d.row_cap);
+            int left = -1, right = -1;
+            for (int k = first; k < n; ++k) {
+                const uint32_t run = row_runs[k];
+                const int rx0 = static_cast<int>(run & 0xffffu);
+                const int rx1 = static_cast<int>(run >> 16);
+                if (rx0 > x1) break;
+                if (d.parent[base + static_cast<uint32_t>(k)] != root) continue;
+                left = left < 0 ? rx0 : min(left, rx0);
+                right = right < 0 ? rx1 : max(right, rx1);
+            }
+            boundary[2 * s] = left < 0 ? kNone : pack_point(left, y);
+            boundary[2 * s + 1] = right < 0 ? kNone : pack_point(right, y);
+        }
+        __syncthreads();
+
+        // Extreme boundary point per direction; the first point wins ties.
+        const int chunk = (points + kFitWarps - 1) / kFitWarps;
+        const int begin = part * chunk;
+        const int end = min(points, begin + chunk);
+        float best_dot = -FLT_MAX;
+        uint32_t best_point = kNone;
+        for (int i = begin; i < end; ++i) {
+            const uint32_t p = boundary[i];
+            if (p == kNone) continue;
+            const float dd = static_cast<float>(p & 0xffffu) * ux + static_cast<float>(p >> 16) * uy;
+            if (dd > best_dot) {
+                best_dot = dd;
+                best_point = p;
+            }
+        }
+        probe_dot[part][dir] = best_dot;
+        probe_point[part][dir] = best_point;
+        __syncthreads();
+        if (tid < kFitDirections) {
+            float best = -FLT_MAX;
+            uint32_t point = kNone;
+            for (int p = 0; p < kFitWarps; ++p) {
+                if (probe_dot[p][tid] > best) {
+                    best = probe_dot[p][tid];
+                    point = probe_point[p][tid];
+                }
+            }
+            extreme[tid] = point;
+        }
+        __syncthreads();
+
+        float* hull_out = d.hull_quads + static_cast<int64_t>(ci) * 8;
+        if (tid == 0) {
+            uint32_t hull[kFitDirections];
+            int hc = 0;
+            for (int i = 0; i < kFitDirections; ++i) {
+                const uint32_t p = extreme[i];
+                if (p == kNone) continue;
+                if (hc > 0 && hull[hc - 1] == p) continue;
+                hull[hc++] = p;
+            }
+            while (hc > 1 && hull[0] == hull[hc - 1]) --hc;
+            float quad[4][2];
+            const bool ok = hull_to_quad(hull, hc, quad);
+            quad_ok = ok ? 1 : 0;
+            const float nan = bdmath::quiet_nan();
+            for (int i = 0; i < 4; ++i) {
+                hull_quad[i][0] = quad[i][0];
+                hull_quad[i][1] = quad[i][1];
+                hull_out[i * 2 + 0] = ok ? quad[i][0] : nan;
+                hull_out[i * 2 + 1] = ok ? quad[i][1] : nan;
+            }
+            if (ok) atomicAdd(&d.state->counts[3], 1u);
+        }
+        __syncthreads();
+
+        const int warp = tid >> 5, lane = tid & 31;
+        for (int fam = 0; fam < 2; ++fam) {
+            if (!(d.families & (1u << fam))) continue;
+            float* out = d.quads + (static_cast<int64_t>(fam) * mc + ci) * 8;
+            if (!quad_ok) {
+                if (tid < 8) out[tid] = bdmath::quiet_nan();
+                continue;
+            }
+            if (tid < 8) fit_quad[tid >> 1][tid & 1] = hull_quad[tid >> 1][tid & 1];
+            __syncthreads();
+            if (d.refine_edges) {
+                for (int iteration = 0; iteration < kFitIterations; ++iteration) {
+                    float line[4];
+                    const bool ok = fit_edge_line_warp(fit_quad, warp, gray, d.width, d.height, stride,
+                                                       family_dim(fam), iteration == 0, lane, line);
+                    if (lane == 0) {
+                        edge_have[warp] = ok ? 1 : 0;
+                        if (ok) {
+                            for (int k = 0; k < 4; ++k) edge_lines[warp][k] = line[k];
+                        }
+                    }
+                    __syncthreads();
+                    if (tid == 0) {
+                        float quad[4][2];
+                        for (int i = 0; i < 4; ++i) {
+                            quad[i][0] = fit_quad[i][0];
+                            quad[i][1] = fit_quad[i][1];
+                        }
+                        refine_moved = apply_refined_lines(quad, edge_lines, edge_have);
+                        for (int i = 0; i < 4; ++i) {
+                            fit_quad[i][0] = quad[i][0];
+                            fit_quad[i][1] = quad[i][1];
+                        }
+                    }
+                    __syncthreads();
+                    if (refine_moved < 0.15f) break;
+                }
+            }
+            if (tid < 8) out[tid] = fit_quad[tid >> 1][tid & 1];
+            __syncthreads();
+        }
+    }
+}
+
+// ===========================================================================
+// 8. Decode (reference homography_from_unit_quad :1249, match_code :1274,
+//    decode_quad :1291, k_decode_quads :1438).  CTA = one (frame, family,
+//    candidate); warp v decodes variant v: rotations 0-3 of the refined quad,
+//    then 0-3 of the hull.
+// ===========================================================================
+__device__ __forceinline__ bool homography_from_unit_quad(const float quad[4][2], float h[9]) {
+    const float x0 = quad[0][0], y0 = quad[0][1];
+    const float x1 = quad[1][0], y1 = quad[1][1];
+    const float x2 = quad[2][0], y2 = quad[2][1];
+    const float x3 = quad[3][0], y3 = quad[3][1];
+    const float dx1 = x1 - x2, dx2 = x3 - x2, dx3 = x0 - x1 + x2 - x3;
+    const float dy1 = y1 - y2, dy2 = y3 - y2, dy3 = y0 - y1 + y2 - y3;
+    const float det = dx1 * dy2 - dx2 * dy1;
+    if (fabsf(det) < 1e-9f) return false;
+    const float g = (dx3 * dy2 - dx2 * dy3) / det;
+    const float k = (dx1 * dy3 - dx3 * dy1) / det;
+    h[0] = x1 - x0 + g * x1;
+    h[1] = x3 - x0 + k * x3;
+    h[2] = x0;
+    h[3] = y1 - y0 + g * y1;
+    h[4] = y3 - y0 + k * y3;
+    h[5] = y0;
+    h[6] = g;
+    h[7] = k;
+    h[8] = 1.0f;
+    return true;
+}
+
+struct VariantResult {
+    int id;
+    int hamming;
+    float margin;
+    float corners[8];
+};
+
+constexpr int kDecodeThreads = 256;
+
+__device__ bool decode_variant_warp(const uint8_t* gray, const FrameDesc& d, int64_t stride,
+                                    int fam, const float* src, int rotation, int lane,
+                                    float* s_raw, float* s_sharp, VariantResult* result) {
+    const int dim = family_dim(fam);
+    const int cells = dim * dim;
+    float corners[4][2];
+    for (int k = 0; k < 4; ++k) {
+        const int s = (rotation + k) & 3;
+        corners[k][0] = src[s * 2 + 0];
+        corners[k][1] = src[s * 2 + 1];
+    }
+    float h[9];
+    if (!homography_from_unit_quad(corners, h)) return false;
+    bool valid = true;
+    float mn = 255.0f, mx = 0.0f;
+    for (int c = lane; c < cells; c += 32) {
+        const int cy = c / dim, cx = c - cy * dim;
+        const float u = (cx + 0.5f) / static_cast<float>(dim);
+        const float v = (cy + 0.5f) / static_cast<float>(dim);
+        const float den = h[6] * u + h[7] * v + 1.0f;
+        if (fabsf(den) < 1e-9f) {
+            valid = false;
+            continue;
+        }
+        const float x = (h[0] * u + h[1] * v + h[2]) / den;
+        const float y = (h[3] * u + h[4] * v + h[5]) / den;
+        const float value = sample_bilinear(gray, d.width, d.height, stride, x - 0.0f, y - 0.0f);
+        if (value < 0.0f) valid = false;
+        s_raw[c] = value;
+        mn = fminf(mn, value);
+        mx = fmaxf(mx, value);
+    }
+    if (!__all_sync(kFull, valid)) return false;
+    for (int off = 16; off > 0; off >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(kFull, mn, off));
+        mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, off));
+    }
+    if (mx - mn < 10.0f) return false;
+    const float thresh = 0.5f * (mn + mx);
+    bool border_bad = false;
+    for (int c = lane; c < cells; c += 32) {
+        const int cy = c / dim, cx = c - cy * dim;
+        if (cx == 0 || cy == 0 || cx == dim - 1 || cy == dim - 1) {
+            border_bad = border_bad || s_raw[c] >= thresh;
+        }
+    }
+    if (__any_sync(kFull, border_bad)) return false;
+    __syncwarp();
+    for (int c = lane; c < cells; c += 32) s_raw[c] = s_raw[c] - thresh;  // diff
+    __syncwarp();
+    const int nbits = (dim - 2) * (dim - 2);
+    uint64_t code_part = 0;
+    for (int c = lane; c < cells; c += 32) {
+        const int cy = c / dim, cx = c - cy * dim;
+        float sv = s_raw[c];
+        if (cx >= 1 && cy >= 1 && cx <= dim - 2 && cy <= dim - 2) {
+            const float cc = s_raw[c];
+            const float lap = 4.0f * cc - s_raw[c - dim] - s_raw[c + dim] - s_raw[c - 1] - s_raw[c + 1];
+            sv = cc + d.sharpening * lap;
+            const int k = (cy - 1) * (dim - 2) + (cx - 1);
+            if (sv > 0.0f) code_part |= 1ull << (nbits - 1 - k);
+        }
+        s_sharp[c] = sv;
+    }
+    for (int off = 16; off > 0; off >>= 1) code_part |= __shfl_xor_sync(kFull, code_part, off);
+    const uint64_t code = code_part;
+
+    // First codeword at the minimum distance: min over (distance, index).
+    const uint64_t* codes = fam == 0 ? d_codes36h11 : d_codes16h5;
+    const int code_count = fam == 0 ? BD_CODEWORDS_36H11_COUNT : BD_CODEWORDS_16H5_COUNT;
+    uint32_t key = 0xffffffffu;
+    for (int i = lane; i < code_count; i += 32) {
+        const uint32_t dist = static_cast<uint32_t>(__popcll(codes[i] ^ code));
+        key = min(key, (dist << 16) | static_cast<uint32_t>(i));
+    }
+    key = __reduce_min_sync(kFull, key);
+    const int best_dist = static_cast<int>(key >> 16);
+    if (best_dist > d.max_hamming[fam]) return false;
+    __syncwarp();
+    if (lane != 0) return true;
+    // Decision margin: sums in row-major order of the data cells.
+    float white_sum = 0.0f, black_sum = 0.0f;
+    int white_count = 0, black_count = 0;
+    for (int cy = 1; cy <= dim - 2; ++cy) {
+        for (int cx = 1; cx <= dim - 2; ++cx) {
+            const float dv = s_sharp[cy * dim + cx];
+            if (dv > 0.0f) {
+                white_sum += dv;
+                ++white_count;
+            } else {
+                black_sum -= dv;
+                ++black_count;
+            }
+        }
+    }
+    const float white_avg = white_sum / static_cast<float>(max(white_count, 1));
+    const float black_avg = black_sum / static_cast<float>(max(black_count, 1));
+    const float margin = fminf(white_avg, black_avg);
+    if (margin < d.min_margin) return false;
+    result->id = static_cast<int>(key & 0xffffu);
+    result->hamming = best_dist;
+    result->margin = margin;
+    for (int k = 0; k < 4; ++k) {
+        result->corners[k * 2 + 0] = corners[k][0];
+        result->corners[k * 2 + 1] = corners[k][1];
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kDecodeThreads) k_decode(const BatchDesc* __restrict__ b,
+                                                           const FrameIO* __restrict__ io) {
+    __shared__ float s_raw[8][64];
+    __shared__ float s_sharp[8][64];
+    __shared__ VariantResult s_res[8];
+    __shared__ int s_ok[8];
+    __shared__ int s_prefix[kMaxFrames + 1];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        int run = 0;
+        for (int f = 0; f < b->frames; ++f) {
+            s_prefix[f] = run;
+            run += static_cast<int>(b->f[f].state->n_candidates) * __popc(b->f[f].families & 3u);
+        }
+        s_prefix[b->frames] = run;
+    }
+    __syncthreads();
+    const int total = s_prefix[b->frames];
+    for (int item = blockIdx.x; item < total; item += gridDim.x) {
+        int fi = 0;
+        while (s_prefix[fi + 1] <= item) ++fi;
+        const FrameDesc& d = b->f[fi];
+        const int n = static_cast<int>(d.state->n_candidates);
+        int local = item - s_prefix[fi];
+        int fam = 0;
+        if (!(d.families & 1u)) {
+            fam = 1;
+        } else if (local >= n) {
+            fam = 1;
+            local -= n;
+        }
+        const int ci = local;
+        const int mc = d.max_candidates;
+        const float* q = d.quads + (static_cast<int64_t>(fam) * mc + ci) * 8;
+        const float* hq = d.hull_quads + static_cast<int64_t>(ci) * 8;
+        DecodeOut* out = d.decodes + static_cast<int64_t>(fam) * mc + ci;
+        if (q[0] != q[0]) {
+            if (tid == 0) out->id = -1;
+            continue;  // uniform across the CTA
+        }
+        const float* src = warp < 4 ? q : hq;
+        const bool ok = decode_variant_warp(io[fi].gray, d, io[fi].stride, fam, src, warp & 3, lane,
+                                            s_raw[warp], s_sharp[warp], &s_res[warp]);
+        if (lane == 0) s_ok[warp] = ok ? 1 : 0;
+        __syncthreads();
+        if (tid == 0) {
+            int best = -1;
+            float best_score = -1.0f;
+            for (int variant = 0; variant < 2 && best < 0; ++variant) {
+                for (int rotation = 0; rotation < 4; ++rotation) {
+                    const int r = variant * 4 + rotation;
+                    if (!s_ok[r]) continue;
+                    const float score =
+                        static_cast<float>(4 - s_res[r].hamming) * 1000.0f + s_res[r].margin;
+                    if (score > best_score) {
+                        best_score = score;
+                        best = r;
+                    }
+                }
+            }
+            if (best < 0) {
+                out->id = -1;
+            } else {
+                out->id = s_res[best].id;
+                out->hamming = s_res[best].hamming;
+                out->margin = s_res[best].margin;
+                for (int k = 0; k < 8; ++k) out->corners[k] = s_res[best].corners[k];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ===========================================================================
+// 9. Finalize one (frame, family): detections in candidate order (first
+//    max_detections), de-duplication, stable sort by id, homography
+//    (reference k_finalize :1542-1601, host fill_homography :1739-1774 --
+//    FP64 here as there).
+// ===========================================================================
+__device__ void fill_homography(const float corners[8], float H[9]) {
+    const double x0 = corners[0], y0 = corners[1];
+    const double x1 = corners[2], y1 = corners[3];
+    const double x2 = corners[4], y2 = corners[5];
+    const double x3 = corners[6], y3 = corners[7];
+    const double dx1 = x1 - x2, dx2 = x3 - x2;
+    const double dx3 = x0 - x1 + x2 - x3;
+    const double dy1 = y1 - y2, dy2 = y3 - y2;
+    const double dy3 = y0 - y1 + y2 - y3;
+    double g = 0.0, h = 0.0;
+    const double det = dx1 * dy2 - dx2 * dy1;
+    if (fabs(det) > 1e-12) {
+        g = (dx3 * dy2 - dx2 * dy3) / det;
+        h = (dx1 * dy3 - dx3 * dy1) / det;
+    }
+    const double a = x1 - x0 + g * x1;
+    const double bb = x3 - x0 + h * x3;
+    const double dd = y1 - y0 + g * y1;
+    const double e = y3 - y0 + h * y3;
+    const double w = g + h + 2.0;
+    const double inv = (fabs(w) > 1e-12) ? 1.0 / w : 0.0;
+    H[0] = static_cast<float>(a * inv);
+    H[1] = static_cast<float>(bb * inv);
+    H[2] = static_cast<float>((a + bb + 2.0 * x0) * inv);
+    H[3] = static_cast<float>(dd * inv);
+    H[4] = static_cast<float>(e * inv);
+    H[5] = static_cast<float>((dd + e + 2.0 * y0) * inv);
+    H[6] = static_cast<float>(g * inv);
+    H[7] = static_cast<float>(h * inv);
+    H[8] = static_cast<float>(w * inv);
+}
+
+constexpr int kFinalThreads = 256;
+
+__global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __restrict__ b) {
+    __shared__ DecodeOut s_in[kMaxDetectionsCap];
+    __shared__ DecodeOut s_out[kMaxDetectionsCap];
+    __shared__ float s_cx[kMaxDetectionsCap], s_cy[kMaxDetectionsCap];
+    __shared__ uint32_t s_warp[kFinalThreads / 32];
+    __shared__ int s_count, s_kept;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int fi = blockIdx.x >> 1;
+    const int fam = blockIdx.x & 1;
+    const FrameDesc& d = b->f[fi];
+    const FrameState* st = d.state;
+    FrameResultHeader* hdr = d.result;
+    if (fam == 0 && tid < 5) hdr->counts[tid] = st->counts[tid];
+    if (fam == 0 && tid == 5) hdr->pad = 0;
+    if (!(d.families & (1u << fam))) {
+        if (tid == 0) hdr->found[fam] = 0;
+        return;
+    }
+    const int n = static_cast<int>(st->n_candidates);
+    const int maxd = d.max_detections;
+    const DecodeOut* dec = d.decodes + static_cast<int64_t>(fam) * d.max_candidates;
+    if (tid == 0) s_count = 0;
+    __syncthreads();
+    // Ordered compaction of the decoded candidates.
+    for (int c = 0; c < n; c += kFinalThreads) {
+        const int i = c + tid;
+        const bool ok = i < n && dec[i].id >= 0;
+        const unsigned bal = __ballot_sync(kFull, ok);
+        if (lane == 0) s_warp[warp] = __popc(bal);
+        __syncthreads();
+        int before = s_count;
+        for (int w2 = 0; w2 < warp; ++w2) before += static_cast<int>(s_warp[w2]);
+        const int pos = before + __popc(bal & lanemask_lt());
+        if (ok && pos < maxd) s_in[pos] = dec[i];
+        __syncthreads();
+        if (tid == 0) {
+            int add = 0;
+            for (int w2 = 0; w2 < kFinalThreads / 32; ++w2) add += static_cast<int>(s_warp[w2]);
+            s_count = s_count + add;
+        }
+        __syncthreads();
+        if (s_count >= maxd) break;
+    }
+    const int m = min(s_count, maxd);
+    // De-duplication in arrival order, one warp.
+    if (warp == 0) {
+        int kept = 0;
+        for (int i = 0; i < m; ++i) {
+            const DecodeOut& dd = s_in[i];
+            float side = 0.0f, cx = 0.0f, cy = 0.0f;
+            for (int k = 0; k < 4; ++k) {
+                const int j = (k + 1) & 3;
+                side += bdmath::hypot(dd.corners[j * 2] - dd.corners[k * 2],
+                                      dd.corners[j * 2 + 1] - dd.corners[k * 2 + 1]);
+                cx += dd.corners[k * 2];
+                cy += dd.corners[k * 2 + 1];
+            }
+            side *= 0.25f;
+            cx *= 0.25f;
+            cy *= 0.25f;
+            const float limit = 0.35f * side;
+            int duplicate = -1;
+            for (int k0 = 0; k0 < kept && duplicate < 0; k0 += 32) {
+                const int k = k0 + lane;
+                const bool hit = k < kept && s_out[k].id == dd.id && fabsf(s_cx[k] - cx) < limit &&
+                                 fabsf(s_cy[k] - cy) < limit;
+                const unsigned bal = __ballot_sync(kFull, hit);
+                if (bal) duplicate = k0 + __ffs(bal) - 1;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                if (duplicate >= 0) {
+                    if (dd.margin > s_out[duplicate].margin) {
+                        s_out[duplicate] = dd;
+                        s_cx[duplicate] = cx;
+                        s_cy[duplicate] = cy;
+                    }
+                } else if (kept < maxd) {
+                    s_out[kept] = dd;
+                    s_cx[kept] = cx;
+                    s_cy[kept] = cy;
+                }
+            }
+            if (duplicate < 0 && kept < maxd) ++kept;
+            __syncwarp();
+        }
+        if (lane == 0) s_kept = kept;
+    }
+    __syncthreads();
+    const int kept = s_kept;
+    bd_detection* dets = result_detections(hdr) + static_cast<int64_t>(fam) * maxd;
+    for (int i = tid; i < kept; i += kFinalThreads) {
+        const int id = s_out[i].id;
+        int rank = 0;
+        for (int j = 0; j < kept; ++j) {
+            const int oj = s_out[j].id;
+            rank += (oj < id || (oj == id && j < i)) ? 1 : 0;
+        }
+        bd_detection r;
+        r.id = id;
+        r.hamming = s_out[i].hamming;
+        r.decision_margin = s_out[i].margin;
+        for (int k = 0; k < 8; ++k) r.corners[k] = s_out[i].corners[k];
+        r.reserved = 0;
+        fill_homography(r.corners, r.homography);
+        dets[rank] = r;
+    }
+    if (tid == 0) hdr->found[fam] = static_cast<uint32_t>(kept);
+}
+
+}  // namespace
+
+void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* io, void* stream_ptr) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream_ptr);
+    const int bands = hd.total_bands;
+    int cand_total = 0;
+    int dec_total = 0;
+    for (int f = 0; f < hd.frames; ++f) {
+        cand_total += hd.f[f].max_candidates;
+        dec_total += hd.f[f].max_candidates * __builtin_popcount(hd.f[f].families & 3u);
+    }
+    const int fit_grid = cand_total < 152 * 8 ? cand_total : 152 * 8;
+    const int dec_grid = dec_total < 152 * 6 ? dec_total : 152 * 6;
+    k_stats<<<bands, 256, 0, s>>>(dd, io);
+    k_binarize_runs<<<bands, 256, 0, s>>>(dd, io);
+    k_merge<<<bands, 256, 0, s>>>(dd);
+    k_region_stats<<<bands, 256, 0, s>>>(dd);
+    k_cand_count<<<bands, 256, 0, s>>>(dd);
+    k_cand_emit<<<bands, 256, 0, s>>>(dd);
+    k_fit<<<fit_grid > 0 ? fit_grid : 1, kFitThreads, 0, s>>>(dd, io);
+    k_decode<<<dec_grid > 0 ? dec_grid : 1, kDecodeThreads, 0, s>>>(dd, io);
+    k_finalize<<<hd.frames * 2, kFinalThreads, 0, s>>>(dd);
+}
+
+}  // namespace bdgb

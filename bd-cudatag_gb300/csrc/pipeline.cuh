@@ -1,0 +1,119 @@
+// Shared layout of the batched detection pipeline: per-frame descriptors,
+// per-frame device state and result records.  Included by the kernels
+// (kernels.cu) and the host engine (engine.cu).
+//
+// One launch of each stage covers every frame of a batch.  A frame is cut
+// into "bands" of 8 pixel rows (one tile row); stages 1-6 run one CTA per
+// band, so a batch of frames of any mix of sizes is one flat grid whose CTAs
+// find their frame by binary search over a prefix of band counts.
+#pragma once
+
+#include <stdint.h>
+
+#include "bdcudatag/bdcudatag.h"
+
+#if defined(__CUDACC__)
+#define BDGB_HD __host__ __device__
+#else
+#define BDGB_HD
+#endif
+
+namespace bdgb {
+
+constexpr int kMaxFrames = 64;         // frames in one batch plan
+constexpr int kTile = 8;               // tile side, pixels
+constexpr int kMinTileContrast = 12;   // reference gpu_detector.cu:39
+constexpr int kFitDirections = 32;     // :46
+constexpr int kMaxBoundaryRows = 1024; // :47
+constexpr int kMaxHullVertices = 64;   // :48
+constexpr int kFitIterations = 2;      // :49
+constexpr int kFitProbeHalf = 24;      // :50
+constexpr int kMaxDetectionsCap = 256;
+constexpr uint32_t kNone = 0xffffffffu;
+
+// Counters and per-frame reductions, zeroed at the start of every batch.
+struct FrameState {
+    uint32_t counts[5];      // [0] candidates (uncapped) [2] runs [3] quads [4] ROI tile rows
+    uint32_t top_enc;        // tile_h - first active tile row (0: none)
+    uint32_t bottom_enc;     // last active tile row + 1 (0: none)
+    uint32_t ref[2];         // noise-floor span quartile, Otsu level
+    uint32_t done_stats;     // CTAs of the stats stage finished
+    uint32_t done_cands;     // CTAs of the candidate-count stage finished
+    uint32_t n_candidates;   // min(counts[0], max_candidates)
+    uint32_t span_hist[256];
+    uint32_t mean_hist[64];
+    uint32_t bin_base[64];   // first flattened position of each area bin
+};
+
+// One decoded candidate (per family): id -1 when nothing decoded.
+struct DecodeOut {
+    int32_t id;
+    int32_t hamming;
+    float margin;
+    float corners[8];
+};
+
+// Result header of one frame; followed by 2 * max_detections bd_detection
+// records (family 0 block, then family 1 block).
+struct FrameResultHeader {
+    uint32_t counts[5];
+    uint32_t found[2];       // detections per family after de-duplication
+    uint32_t pad;
+};
+
+// Input of one frame for one call: device pointer and row stride.
+struct FrameIO {
+    const uint8_t* gray;
+    int64_t stride;
+};
+
+struct FrameDesc {
+    int32_t width, height;
+    int32_t tile_w, tile_h, words, row_cap;
+    int32_t max_candidates, max_detections;
+    uint32_t families;             // bit f set: decode family f
+    int32_t min_cluster_pixels, min_tag_pixels, refine_edges;
+    int32_t max_hamming[2];
+    float min_margin, sharpening;
+    // device buffers of this frame
+    uint8_t* tile_min;             // tile_w * tile_h
+    uint8_t* tile_max;
+    int32_t* row_lo;               // first / last contrasting tile per tile row (-1: none)
+    int32_t* row_hi;
+    uint32_t* bits;                // height * words, 1 = white
+    uint32_t* row_count;           // height
+    uint32_t* runs;                // slots (height * row_cap): x0 | x1 << 16
+    uint32_t* parent;              // slots: union-find, then the root of every run
+    uint32_t* area;                // slots (valid at roots)
+    uint32_t* bbox;                // 4 * slots (valid at roots)
+    uint32_t* cand_meta;           // slots: bin << 24 | rank in band, or kNone
+    uint32_t* band_bins;           // tile_h * 64 candidate counts, then exclusive prefixes
+    uint32_t* candidates;          // max_candidates root slots, canonical order
+    FrameState* state;
+    float* hull_quads;             // max_candidates * 8
+    float* quads;                  // 2 * max_candidates * 8 (per family)
+    DecodeOut* decodes;            // 2 * max_candidates
+    FrameResultHeader* result;     // header + 2 * max_detections records
+};
+
+struct BatchDesc {
+    int32_t frames;
+    int32_t total_bands;
+    int32_t band_prefix[kMaxFrames + 1];  // exclusive prefix of tile_h over frames
+    FrameDesc f[kMaxFrames];
+};
+
+BDGB_HD inline bd_detection* result_detections(FrameResultHeader* h) {
+    return reinterpret_cast<bd_detection*>(h + 1);
+}
+
+BDGB_HD inline size_t result_bytes(int max_detections) {
+    return sizeof(FrameResultHeader) + 2 * static_cast<size_t>(max_detections) * sizeof(bd_detection);
+}
+
+// Launch sequence of one batch on one stream (kernels.cu).  `io` is a
+// device array of FrameIO, one per frame.
+void enqueue_pipeline(const BatchDesc* device_desc, const BatchDesc& host_desc,
+                      const FrameIO* device_io, void* stream);
+
+}  // namespace bdgb

@@ -1,0 +1,104 @@
+/*
+ * bdcudatag GB300 additions.  These entry points have no counterpart in the
+ * reference C ABI; the reference symbols in bdcudatag.h are unchanged.
+ *
+ * Batches: a bd_batch is a fixed set of cameras (frame size + family set)
+ * whose frames are detected together, one launch per pipeline stage for the
+ * whole set, replayed as one CUDA graph.  Each camera's results are exactly
+ * what a bd_detector of that size and family returns for the same frame.
+ */
+#ifndef BDCUDATAG_BDCUDATAG_GB300_H
+#define BDCUDATAG_BDCUDATAG_GB300_H
+
+#include <stdint.h>
+
+#include "bdcudatag/bdcudatag.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BD_BATCH_MAX_CAMERAS 64
+#define BD_FAMILY_MASK(f) (1u << (f))
+
+typedef struct bd_batch bd_batch;
+
+/* One camera of a batch, 16 bytes.  families is a mask of
+ * BD_FAMILY_MASK(BD_FAMILY_TAG36H11) and/or BD_FAMILY_MASK(BD_FAMILY_TAG16H5);
+ * stages up to candidate selection run once per frame, quad refinement and
+ * decoding once per requested family. */
+typedef struct bd_camera {
+    int32_t width;
+    int32_t height;
+    uint32_t families;
+    int32_t reserved;
+} bd_camera;
+
+/* Creates a batch of `count` cameras (1..64).  All device and pinned memory
+ * is allocated here.  NULL on failure, with *status_out and bd_last_error()
+ * set as for bd_detector_create. */
+BD_API bd_batch* bd_batch_create(const bd_camera* cameras, int32_t count, const bd_config* config,
+                                 int32_t* status_out);
+BD_API void bd_batch_destroy(bd_batch* batch);
+BD_API int32_t bd_batch_camera_count(const bd_batch* batch);
+BD_API int32_t bd_batch_max_detections(const bd_batch* batch);
+/* Device memory held by the batch, in bytes. */
+BD_API int64_t bd_batch_device_bytes(const bd_batch* batch);
+
+/*
+ * Detects one frame per camera.  frames[i] (row stride strides[i] >= width)
+ * is camera i's 8-bit frame: host memory for _host, device memory of the
+ * batch's CUDA context for _device.  out receives count * 2 * max_detections
+ * records laid out [camera][family][max_detections]; found receives
+ * count * 2 entries: the number of detections of camera i, family f at
+ * found[2 * i + f] (sorted by id as bd_detector_detect_host), or -1 when the
+ * camera does not request that family.  Returns BD_OK or a negative
+ * bd_status.
+ */
+BD_API int32_t bd_batch_detect_host(bd_batch* batch, const uint8_t* const* frames,
+                                    const int32_t* strides, bd_detection* out, int32_t* found);
+BD_API int32_t bd_batch_detect_device(bd_batch* batch, const uint8_t* const* frames,
+                                      const int32_t* strides, bd_detection* out, int32_t* found);
+
+/* Split form of the calls above: submit enqueues the batch and returns at
+ * once; wait blocks until it finishes and writes out / found.  One batch may
+ * be in flight per bd_batch; use several batches to overlap. */
+BD_API int32_t bd_batch_submit_host(bd_batch* batch, const uint8_t* const* frames,
+                                    const int32_t* strides);
+BD_API int32_t bd_batch_submit_device(bd_batch* batch, const uint8_t* const* frames,
+                                      const int32_t* strides);
+BD_API int32_t bd_batch_wait(bd_batch* batch, bd_detection* out, int32_t* found);
+
+/* Pinned host staging buffer of camera i (width * height bytes, stride =
+ * width).  A frame written here is submitted without the staging copy by
+ * passing this pointer as frames[i]. */
+BD_API uint8_t* bd_batch_host_frame(bd_batch* batch, int32_t camera);
+
+/* GPU time of the last completed batch (events around the graph), ms. */
+BD_API float bd_batch_last_gpu_ms(const bd_batch* batch);
+
+/* Pipeline counters of camera i in the last batch: [0] candidates before
+ * the cap, [1] 0, [2] runs, [3] quads, [4] ROI tile rows. */
+BD_API int32_t bd_batch_counts(const bd_batch* batch, int32_t camera, uint32_t counts[5]);
+
+/*
+ * Test hook: copies a named intermediate buffer of camera i of the last
+ * batch (for a bd_detector: its single frame) into dst.  Returns the
+ * buffer's size in bytes, or -1 for an unknown name.  Names: tile_min,
+ * tile_max, bits, row_count, runs, label, area, bbox, candidates,
+ * hull_quads, quads, decodes, state.
+ */
+BD_API int64_t bd_batch_debug_stage(bd_batch* batch, int32_t camera, const char* name, void* dst,
+                                    int64_t dst_bytes);
+BD_API int64_t bd_detector_debug_stage(bd_detector* detector, const char* name, void* dst,
+                                       int64_t dst_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#ifdef __cplusplus
+static_assert(sizeof(bd_camera) == 16, "bd_camera layout changed");
+#endif
+
+#endif /* BDCUDATAG_BDCUDATAG_GB300_H */

@@ -22,6 +22,9 @@ namespace {
 
 #include "../bd-cudatag_gb300/csrc/families_data.inc"
 
+const uint64_t kCodewords36h11[BD_CODEWORDS_36H11_COUNT] = {BD_CODEWORDS_36H11};
+const uint64_t kCodewords16h5[BD_CODEWORDS_16H5_COUNT] = {BD_CODEWORDS_16H5};
+
 struct Family {
     const char* name;
     int bits_per_side;

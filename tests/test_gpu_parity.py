@@ -1,0 +1,221 @@
+"""CUDA pipeline versus the CPU oracle, through the C ABI (gpu).
+
+Bit-exact: the bitmap, runs, component labels, area/bbox at roots, the
+candidate list, hull and refined quads, per-candidate decodes and the final
+records (id, hamming, margin, corners, homography).  The oracle is pinned to
+the reference in test_oracle_pin.py.
+"""
+import numpy as np
+import pytest
+
+import bdcudatag
+import oracle
+import scenes
+from helpers import kat_multiple_frame, pose_corners, score
+
+pytestmark = pytest.mark.gpu
+W, H = 640, 480
+
+
+def kat_config(**kw):
+    return bdcudatag.default_config(max_detections=32, min_decision_margin=2.0, **kw)
+
+
+def okat_config(**kw):
+    return oracle.default_config(max_detections=32, min_decision_margin=2.0, **kw)
+
+
+def same_records(a, b):
+    assert a.shape == b.shape
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), (a, b)
+
+
+def check_frame(img, family=0, gcfg=None, ocfg=None, stages=True):
+    """GPU single-frame detect equals the oracle at every stage."""
+    h, w = img.shape
+    det = bdcudatag.Detector(family, w, h, gcfg)
+    n, got = det.detect(img)
+    ref = oracle.Frame(img, family, ocfg)
+    wn, want = ref.detections()
+    assert n == wn
+    same_records(got, want)
+    if stages:
+        rc = det.stage("row_count")
+        assert np.array_equal(rc, ref.stage("row_count"))
+        assert np.array_equal(det.stage("bits"), ref.stage("bits"))
+        valid = np.zeros((h, ref.row_cap), bool)
+        valid[np.arange(ref.row_cap)[None, :] < rc[:, None]] = True
+        valid = valid.ravel()
+        assert np.array_equal(det.stage("runs")[valid], ref.stage("runs")[valid])
+        lab = det.stage("label")[valid]
+        assert np.array_equal(lab, ref.stage("label")[valid])
+        roots = np.unique(lab)
+        assert np.array_equal(det.stage("area")[roots], ref.stage("area")[roots])
+        assert np.array_equal(det.stage("bbox").reshape(-1, 4)[roots], ref.stage("bbox").reshape(-1, 4)[roots])
+        nc = ref.candidate_count
+        assert np.array_equal(det.stage("candidates")[:nc], ref.stage("candidates"))
+        hq = det.stage("hull_quads")[:nc * 8]
+        assert np.array_equal(hq.view(np.uint32), ref.stage("hull_quads")[:nc * 8].view(np.uint32))
+        q = det.stage("quads")[family * ref.max_candidates * 8:][:nc * 8]
+        assert np.array_equal(q.view(np.uint32), ref.stage("quads")[:nc * 8].view(np.uint32))
+        dg = det.stage("decodes")[family * ref.max_candidates:][:nc]
+        do = ref.stage("decodes")
+        assert np.array_equal(dg["id"], do["id"])
+        ok = do["id"] >= 0
+        assert np.array_equal(dg[ok].view(np.uint8), do[ok].view(np.uint8))
+    st = det.stats()
+    c = ref.counts()
+    assert st.runs == c[2] and st.quads == c[3] and st.detections == wn
+    assert st.candidates == min(c[0], ref.max_candidates)
+    assert st.roi_rows == min(c[4] * 8, h)
+    return n, got
+
+
+# --- the reference's own known-answer tests (test_detector.cpp) -------------
+
+@pytest.mark.parametrize("family,tag_id,size", [(0, 0, 170), (1, 0, 120)])
+def test_centered_tag(family, tag_id, size):
+    pose = scenes.make_pose(W * 0.5, H * 0.5, size, 0.0)
+    n, d = check_frame(scenes.render_tag(family, tag_id, W, H, pose), family, kat_config(), okat_config())
+    assert n == 1 and d["id"][0] == tag_id and d["hamming"][0] == 0 and d["decision_margin"][0] > 2.0
+    assert np.abs(d["corners"][0].reshape(4, 2) - pose_corners(pose)).max() <= 2.5
+
+
+def test_rotations_hamming_small_homography():
+    for r in range(4):
+        pose = scenes.make_pose(W * 0.5, H * 0.5, 170.0, r * 1.5707963267948966)
+        n, d = check_frame(scenes.render_tag(0, 0, W, H, pose), 0, kat_config(), okat_config())
+        assert n == 1 and d["id"][0] == 0
+    pose = scenes.make_pose(W * 0.5, H * 0.5, 170.0, 0.15)
+    img = scenes.render_tag(0, 0, W, H, pose, flip_one_bit=True)
+    n, d = check_frame(img, 0, kat_config(), okat_config())
+    assert n == 1 and d["hamming"][0] == 1
+    n, _ = check_frame(img, 0, kat_config(max_hamming=0), okat_config(max_hamming=0))
+    assert n == 0
+    pose = scenes.make_pose(W * 0.5, H * 0.5, 38.0, 0.25)
+    n, d = check_frame(scenes.render_tag(0, 7, W, H, pose), 0, kat_config(), okat_config())
+    assert n == 1 and d["id"][0] == 7
+    pose = scenes.make_pose(W * 0.5, H * 0.5, 170.0, 0.3, 0.00035)
+    n, d = check_frame(scenes.render_tag(0, 5, W, H, pose), 0, kat_config(), okat_config())
+    Hm = d["homography"][0].astype(np.float64)
+    assert abs(Hm[8] - 1.0) <= 1e-5
+    c = d["corners"][0].reshape(4, 2)
+    for i, (tx, ty) in enumerate([(-1, -1), (1, -1), (1, 1), (-1, 1)]):
+        w = Hm[6] * tx + Hm[7] * ty + Hm[8]
+        assert abs((Hm[0] * tx + Hm[1] * ty + Hm[2]) / w - c[i, 0]) <= 0.01
+
+
+def test_multiple_and_blank():
+    img, poses = kat_multiple_frame()
+    n, d = check_frame(img, 0, kat_config(), okat_config())
+    assert n == 5 and sorted(d["id"]) == sorted(poses)
+    det = bdcudatag.Detector(0, W, H, kat_config())
+    for v in (255, 0):
+        n, _ = det.detect(np.full((H, W), v, np.uint8))
+        assert n == 0
+    assert det.stats().roi_rows == 0
+
+
+def test_device_path_and_stride():
+    torch = pytest.importorskip("torch")
+    pose = scenes.make_pose(W * 0.5, H * 0.5, 150.0, 0.1)
+    img = scenes.render_tag(0, 11, W, H, pose)
+    det = bdcudatag.Detector(0, W, H, kat_config())
+    n_host, host = det.detect(img)
+    padded = np.full((H, W + 96), 7, np.uint8)
+    padded[:, :W] = img
+    t = torch.from_numpy(padded).cuda()
+    n, dev = det.detect_device(t, W + 96)
+    assert n == n_host == 1 and dev["id"][0] == 11
+    same_records(dev, host)
+    n2, strided = det.detect(padded[:, :W], stride=W + 96)
+    same_records(strided, host)
+
+
+def test_thread_safety():
+    import threading
+    pose = scenes.make_pose(W * 0.5, H * 0.5, 170.0, 0.0)
+    img = scenes.render_tag(0, 0, W, H, pose)
+    det = bdcudatag.Detector(0, W, H, kat_config())
+    bad = []
+
+    def work():
+        local = bdcudatag.Detection()
+        for _ in range(5):
+            n = bdcudatag.lib().bd_detector_detect_host(det.handle, img.ctypes.data, W,
+                                                        bdcudatag.ctypes.addressof(local), 1)
+            if n != 1 or local.id != 0:
+                bad.append(n)
+
+    threads = [threading.Thread(target=work) for _ in range(4)]
+    [t.start() for t in threads]
+    [t.join() for t in threads]
+    assert not bad and det.stats().frames == 20
+
+
+# --- the reference's benchmark scenes: bit-exact and published accuracy ------
+
+@pytest.mark.parametrize("w,h", [(640, 480), (1280, 720), (1280, 800), (1920, 1080)])
+def test_reference_scenes(w, h):
+    imgs, ids, corners = scenes.ref_scenes(w, h, 8)
+    tags = found = wrong = 0
+    errs = []
+    for i in range(len(imgs)):
+        n, d = check_frame(imgs[i], 0, bdcudatag.default_config(max_detections=32),
+                           oracle.default_config(max_detections=32), stages=(i < 2))
+        t, f, wr, e = score(d, n, ids[i], corners[i])
+        tags, found, wrong, errs = tags + t, found + f, wrong + wr, errs + e
+    assert found == tags and wrong == 0
+    assert np.median(errs) < 0.3
+
+
+# --- workload frames and edge cases -------------------------------------------
+
+@pytest.mark.parametrize("index", range(8))
+def test_config2_frames_both_families(index):
+    img, truth = scenes.render_config(2, index, 1280, 800)
+    for fam in (0, 1):
+        check_frame(img, fam, stages=(index % 4 == 0 or index == 5))
+
+
+@pytest.mark.parametrize("w,h", [(16, 16), (17, 23), (1001, 777), (33, 300), (2000, 40)])
+def test_odd_sizes(w, h):
+    img, _ = scenes.render_config(3, w * 7 + h, w, h)
+    check_frame(img, 0)
+    check_frame(np.ascontiguousarray(img[::-1]), 1)
+
+
+def test_caps_exceeded():
+    # Clutter frame (index 5) pushes candidates past a small cap; a tiny
+    # detection cap truncates in candidate order.
+    img, _ = scenes.render_config(2, 5, 1280, 800)
+    check_frame(img, 0, bdcudatag.default_config(max_candidates=16, max_detections=2),
+                oracle.default_config(max_candidates=16, max_detections=2))
+    det = bdcudatag.Detector(0, 1280, 800, bdcudatag.default_config(max_detections=4))
+    n, d = det.detect(img, capacity=0)
+    assert len(d) == 0 and n == oracle.Frame(img, 0, oracle.default_config(max_detections=4)).detections()[0]
+
+
+def test_batch_matches_single_frames():
+    sizes = [(640, 480), (1280, 800), (1600, 1304), (1920, 1080)] * 2
+    frames, _ = scenes.render_many(3, sizes, threads=8)
+    cams = [(w, h, 3 if i % 3 else 1) for i, (w, h) in enumerate(sizes)]
+    batch = bdcudatag.Batch(cams)
+    found, out = batch.detect(frames)
+    for i, (w, h, fams) in enumerate(cams):
+        for fam in (0, 1):
+            if not (fams >> fam) & 1:
+                assert found[i, fam] == -1
+                continue
+            wn, want = oracle.Frame(frames[i], fam).detections()
+            assert found[i, fam] == wn
+            same_records(out[i, fam, :wn], want)
+    # device input, second call on the same plan
+    torch = pytest.importorskip("torch")
+    dev = [torch.from_numpy(f).cuda() for f in frames]
+    found2, out2 = batch.detect(dev, strides=[w for w, _ in sizes], device=True)
+    assert np.array_equal(found2, found)
+    for i in range(len(cams)):
+        for fam in (0, 1):
+            if found[i, fam] > 0:
+                same_records(out2[i, fam, :found[i, fam]], out[i, fam, :found[i, fam]])

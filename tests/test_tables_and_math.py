@@ -13,12 +13,13 @@ INC = Path(__file__).resolve().parent.parent / "bd-cudatag_gb300" / "csrc" / "fa
 def load_tables():
     text = INC.read_text()
     out = {}
-    for name in ("kCodewords36h11", "kCodewords16h5"):
-        body = re.search(name + r"\[(\d+)\] = \{(.*?)\};", text, re.S)
-        vals = [int(v, 16) for v in re.findall(r"0x([0-9a-f]+)ull", body.group(2))]
-        assert len(vals) == int(body.group(1))
+    for name in ("BD_CODEWORDS_36H11", "BD_CODEWORDS_16H5"):
+        count = int(re.search(r"#define %s_COUNT (\d+)" % name, text).group(1))
+        body = text.split("#define %s \\" % name, 1)[1].split("#define", 1)[0]
+        vals = [int(v, 16) for v in re.findall(r"0x([0-9a-f]+)ull", body)]
+        assert len(vals) == count
         out[name] = vals
-    return out["kCodewords36h11"], out["kCodewords16h5"]
+    return out["BD_CODEWORDS_36H11"], out["BD_CODEWORDS_16H5"]
 
 
 def rotate(codes: np.ndarray, bits: int) -> np.ndarray:
