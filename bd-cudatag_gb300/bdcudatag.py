@@ -86,6 +86,8 @@ GB300_SYMBOLS = [
     "bd_batch_device_bytes", "bd_batch_detect_host", "bd_batch_detect_device",
     "bd_batch_submit_host", "bd_batch_submit_device", "bd_batch_wait", "bd_batch_host_frame",
     "bd_batch_last_gpu_ms", "bd_batch_counts", "bd_batch_debug_stage", "bd_detector_debug_stage",
+    "bd_batch_set_stream", "bd_stage_count", "bd_stage_name", "bd_batch_profile_device",
+    "bd_batch_query",
 ]
 
 _LIB = None
@@ -140,6 +142,12 @@ def lib() -> ctypes.CDLL:
         L.bd_batch_debug_stage.restype = ctypes.c_int64
         L.bd_detector_debug_stage.argtypes = [_P, ctypes.c_char_p, _P, ctypes.c_int64]
         L.bd_detector_debug_stage.restype = ctypes.c_int64
+        L.bd_batch_set_stream.argtypes = [_P, _P]
+        L.bd_stage_name.restype = ctypes.c_char_p
+        L.bd_stage_name.argtypes = [ctypes.c_int32]
+        L.bd_batch_profile_device.argtypes = [_P, _P, _P, _P]
+        L.bd_batch_query.argtypes = [_P]
+        L.bd_batch_query.restype = ctypes.c_int32
         _LIB = L
     return _LIB
 
@@ -279,6 +287,27 @@ class Batch:
         if rc != 0:
             raise RuntimeError(f"batch wait failed ({rc}): {last_error()}")
         return (self.found.copy(), self.out.copy()) if copy else (self.found, self.out)
+
+    def set_stream(self, stream) -> None:
+        """stream: a torch.cuda.Stream, an int handle or None."""
+        handle = 0 if stream is None else (stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+        lib().bd_batch_set_stream(self.handle, handle or None)
+
+    def profile_device(self, frames, strides=None) -> dict:
+        self._set(frames, strides)
+        n = lib().bd_stage_count()
+        ms = np.zeros(n, dtype=np.float32)
+        rc = lib().bd_batch_profile_device(self.handle, ctypes.cast(self._ptrs, _P),
+                                           self._strides.ctypes.data, ms.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"profile failed ({rc}): {last_error()}")
+        return {lib().bd_stage_name(i).decode(): float(ms[i]) for i in range(n)}
+
+    def query(self) -> bool:
+        r = lib().bd_batch_query(self.handle)
+        if r < 0:
+            raise RuntimeError(f"batch query failed ({r}): {last_error()}")
+        return r == 1
 
     def host_frame(self, i: int) -> np.ndarray:
         w, h, _ = self.cameras[i]

@@ -405,6 +405,21 @@ int32_t bd_batch_wait(bd_batch* batch, bd_detection* out, int32_t* found) {
     return batch_collect(batch, out, found);
 }
 
+int32_t bd_batch_query(bd_batch* batch) {
+    if (!batch) {
+        set_error("null batch");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    std::string error;
+    const int r = batch->plan->query(&error);
+    if (r < 0) {
+        set_error(error);
+        return BD_ERROR_CUDA;
+    }
+    return r;
+}
+
 int32_t bd_batch_detect_host(bd_batch* batch, const uint8_t* const* frames, const int32_t* strides,
                              bd_detection* out, int32_t* found) {
     const int rc = bd_batch_submit_host(batch, frames, strides);
@@ -417,6 +432,40 @@ int32_t bd_batch_detect_device(bd_batch* batch, const uint8_t* const* frames,
     const int rc = bd_batch_submit_device(batch, frames, strides);
     if (rc != BD_OK) return rc;
     return bd_batch_wait(batch, out, found);
+}
+
+int32_t bd_batch_set_stream(bd_batch* batch, void* cuda_stream) {
+    if (!batch) {
+        set_error("null batch");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    batch->plan->set_stream(cuda_stream);
+    return BD_OK;
+}
+
+int32_t bd_stage_count(void) { return bdgb::kStageCount; }
+
+const char* bd_stage_name(int32_t stage) {
+    if (stage < 0 || stage >= bdgb::kStageCount) return nullptr;
+    return bdgb::kStageNames[stage];
+}
+
+int32_t bd_batch_profile_device(bd_batch* batch, const uint8_t* const* frames,
+                                const int32_t* strides, float* stage_ms) {
+    const int bad = batch_check(batch, frames, strides);
+    if (bad != BD_OK) return bad;
+    if (!stage_ms) {
+        set_error("null stage time array");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    std::string error;
+    if (batch->plan->profile_device(frames, strides, stage_ms, &error) != 0) {
+        set_error(error);
+        return BD_ERROR_CUDA;
+    }
+    return BD_OK;
 }
 
 uint8_t* bd_batch_host_frame(bd_batch* batch, int32_t camera) {

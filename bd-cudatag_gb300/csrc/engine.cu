@@ -81,14 +81,24 @@ struct Plan::Impl {
     uint8_t* results_pinned = nullptr;
     size_t results_bytes = 0;
     size_t result_stride = 0;
-    cudaGraphExec_t graph_host = nullptr;
-    cudaGraphExec_t graph_device = nullptr;
+    cudaGraphExec_t graph_host = nullptr;    // H2D of the staging buffer + pipeline + D2H
+    cudaGraphExec_t graph_fixed = nullptr;   // pipeline + D2H on the plan's device frames
+    cudaGraphExec_t graph_device = nullptr;  // caller device frames
+    cudaStream_t user_stream = nullptr;      // caller stream for submits (null: own stream)
+    cudaEvent_t stage_events[kStageCount + 1] = {};
     bool pending = false;
+
+    cudaStream_t active() const { return user_stream ? user_stream : stream; }
 
     ~Impl() {
         if (stream) cudaStreamSynchronize(stream);
+        if (user_stream) cudaStreamSynchronize(user_stream);
         if (graph_host) cudaGraphExecDestroy(graph_host);
+        if (graph_fixed) cudaGraphExecDestroy(graph_fixed);
         if (graph_device) cudaGraphExecDestroy(graph_device);
+        for (cudaEvent_t e : stage_events) {
+            if (e) cudaEventDestroy(e);
+        }
         if (ev_start) cudaEventDestroy(ev_start);
         if (ev_stop) cudaEventDestroy(ev_stop);
         if (stream) cudaStreamDestroy(stream);
@@ -98,27 +108,35 @@ struct Plan::Impl {
         if (io_staging) cudaFreeHost(io_staging);
     }
 
-    void enqueue_host() {
-        cudaMemcpyAsync(frames_dev, frames_pinned, frame_bytes, cudaMemcpyHostToDevice, stream);
-        cudaMemsetAsync(states, 0, states_bytes, stream);
-        enqueue_pipeline(dev_desc, host_desc, io_fixed, stream);
-        cudaMemcpyAsync(results_pinned, results_dev, results_bytes, cudaMemcpyDeviceToHost, stream);
+    // mode 0: staging H2D + pipeline on the plan's frames; 1: pipeline on
+    // the plan's frames (inputs already copied); 2: caller device frames.
+    void enqueue(int mode, cudaStream_t s, void* const* events = nullptr) {
+        if (mode == 0) {
+            cudaMemcpyAsync(frames_dev, frames_pinned, frame_bytes, cudaMemcpyHostToDevice, s);
+        } else if (mode == 2) {
+            cudaMemcpyAsync(io_caller, io_staging, sizeof(FrameIO) * host_desc.frames,
+                            cudaMemcpyHostToDevice, s);
+        }
+        cudaMemsetAsync(states, 0, states_bytes, s);
+        enqueue_pipeline(dev_desc, host_desc, mode == 2 ? io_caller : io_fixed, s, events);
+        cudaMemcpyAsync(results_pinned, results_dev, results_bytes, cudaMemcpyDeviceToHost, s);
     }
 
-    void enqueue_device() {
-        cudaMemcpyAsync(io_caller, io_staging, sizeof(FrameIO) * host_desc.frames,
-                        cudaMemcpyHostToDevice, stream);
-        cudaMemsetAsync(states, 0, states_bytes, stream);
-        enqueue_pipeline(dev_desc, host_desc, io_caller, stream);
-        cudaMemcpyAsync(results_pinned, results_dev, results_bytes, cudaMemcpyDeviceToHost, stream);
+    void launch(int mode, cudaStream_t s) {
+        cudaGraphExec_t g = mode == 0 ? graph_host : (mode == 1 ? graph_fixed : graph_device);
+        if (g) {
+            cudaGraphLaunch(g, s);
+        } else {
+            enqueue(mode, s);
+        }
     }
 
-    bool capture(bool device_mode, cudaGraphExec_t* out) {
+    bool capture(int mode, cudaGraphExec_t* out) {
         if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             cudaGetLastError();
             return false;
         }
-        if (device_mode) enqueue_device(); else enqueue_host();
+        enqueue(mode, stream);
         cudaGraph_t graph = nullptr;
         if (cudaStreamEndCapture(stream, &graph) != cudaSuccess || !graph) {
             cudaGetLastError();
@@ -309,8 +327,9 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     if (config.use_graph) {
         // A failed capture falls back to direct launches (reference
         // gpu_detector.cu:2051-2056).
-        if (!im.capture(false, &im.graph_host)) im.graph_host = nullptr;
-        if (!im.capture(true, &im.graph_device)) im.graph_device = nullptr;
+        if (!im.capture(0, &im.graph_host)) im.graph_host = nullptr;
+        if (!im.capture(1, &im.graph_fixed)) im.graph_fixed = nullptr;
+        if (!im.capture(2, &im.graph_device)) im.graph_device = nullptr;
     }
     return plan;
 }
@@ -327,6 +346,12 @@ int Plan::submit_host(const uint8_t* const* frames, const int32_t* strides, std:
         if (error) *error = "a batch is already in flight";
         return -1;
     }
+    const cudaStream_t s = im.active();
+    // Frames in page-locked memory are copied by DMA straight from the
+    // caller; others are compacted into the pinned staging buffer first (the
+    // reference's detect_host path, gpu_detector.cu:2169-2176).
+    bool direct[kMaxFrames] = {};
+    bool any_direct = false;
     for (int i = 0; i < this->frames(); ++i) {
         const int w = frames_[i].width, h = frames_[i].height;
         uint8_t* dst = im.frames_pinned + im.frame_offset[i];
@@ -334,7 +359,14 @@ int Plan::submit_host(const uint8_t* const* frames, const int32_t* strides, std:
             if (error) *error = "null image pointer";
             return -1;
         }
-        if (frames[i] == dst) continue;  // rendered in place
+        if (frames[i] == dst) continue;  // already in the staging buffer
+        cudaPointerAttributes attr;
+        if (cudaPointerGetAttributes(&attr, frames[i]) == cudaSuccess &&
+            attr.type == cudaMemoryTypeHost) {
+            direct[i] = any_direct = true;
+            continue;
+        }
+        cudaGetLastError();
         if (strides[i] == w) {
             std::memcpy(dst, frames[i], static_cast<size_t>(w) * h);
         } else {
@@ -344,17 +376,28 @@ int Plan::submit_host(const uint8_t* const* frames, const int32_t* strides, std:
             }
         }
     }
-    cudaEventRecord(im.ev_start, im.stream);
-    if (im.graph_host) {
-        const cudaError_t st = cudaGraphLaunch(im.graph_host, im.stream);
-        if (st != cudaSuccess) {
-            if (error) *error = cuda_error("cudaGraphLaunch", st);
-            return -1;
-        }
+    cudaEventRecord(im.ev_start, s);
+    if (!any_direct) {
+        im.launch(0, s);
     } else {
-        im.enqueue_host();
+        for (int i = 0; i < this->frames(); ++i) {
+            const int w = frames_[i].width, h = frames_[i].height;
+            uint8_t* dev = im.frames_dev + im.frame_offset[i];
+            if (direct[i]) {
+                cudaMemcpy2DAsync(dev, w, frames[i], strides[i], w, h, cudaMemcpyHostToDevice, s);
+            } else {
+                cudaMemcpyAsync(dev, im.frames_pinned + im.frame_offset[i], static_cast<size_t>(w) * h,
+                                cudaMemcpyHostToDevice, s);
+            }
+        }
+        im.launch(1, s);
     }
-    cudaEventRecord(im.ev_stop, im.stream);
+    cudaEventRecord(im.ev_stop, s);
+    const cudaError_t st = cudaGetLastError();
+    if (st != cudaSuccess) {
+        if (error) *error = cuda_error("cudaGraphLaunch", st);
+        return -1;
+    }
     im.pending = true;
     return 0;
 }
@@ -373,18 +416,47 @@ int Plan::submit_device(const uint8_t* const* frames, const int32_t* strides, st
         im.io_staging[i].gray = frames[i];
         im.io_staging[i].stride = strides[i];
     }
-    cudaEventRecord(im.ev_start, im.stream);
-    if (im.graph_device) {
-        const cudaError_t st = cudaGraphLaunch(im.graph_device, im.stream);
-        if (st != cudaSuccess) {
-            if (error) *error = cuda_error("cudaGraphLaunch", st);
+    const cudaStream_t s = im.active();
+    cudaEventRecord(im.ev_start, s);
+    im.launch(2, s);
+    cudaEventRecord(im.ev_stop, s);
+    const cudaError_t st = cudaGetLastError();
+    if (st != cudaSuccess) {
+        if (error) *error = cuda_error("cudaGraphLaunch", st);
+        return -1;
+    }
+    im.pending = true;
+    return 0;
+}
+
+void Plan::set_stream(void* stream) {
+    impl_->user_stream = static_cast<cudaStream_t>(stream);
+}
+
+int Plan::profile_device(const uint8_t* const* frames, const int32_t* strides, float* stage_ms,
+                         std::string* error) {
+    Impl& im = *impl_;
+    if (im.pending && wait(error) != 0) return -1;
+    for (int k = 0; k <= kStageCount; ++k) {
+        if (!im.stage_events[k] && cudaEventCreate(&im.stage_events[k]) != cudaSuccess) {
+            if (error) *error = "cudaEventCreate failed";
             return -1;
         }
-    } else {
-        im.enqueue_device();
     }
-    cudaEventRecord(im.ev_stop, im.stream);
-    im.pending = true;
+    for (int i = 0; i < this->frames(); ++i) {
+        im.io_staging[i].gray = frames[i];
+        im.io_staging[i].stride = strides[i];
+    }
+    const cudaStream_t s = im.active();
+    im.enqueue(2, s, reinterpret_cast<void* const*>(im.stage_events));
+    const cudaError_t st = cudaStreamSynchronize(s);
+    if (st != cudaSuccess) {
+        if (error) *error = cuda_error("cudaStreamSynchronize", st);
+        return -1;
+    }
+    for (int k = 0; k < kStageCount; ++k) {
+        cudaEventElapsedTime(&stage_ms[k], im.stage_events[k], im.stage_events[k + 1]);
+    }
     return 0;
 }
 
@@ -406,6 +478,16 @@ int Plan::wait(std::string* error) {
         return -1;
     }
     return 0;
+}
+
+int Plan::query(std::string* error) {
+    Impl& im = *impl_;
+    if (!im.pending) return 1;
+    const cudaError_t st = cudaEventQuery(im.ev_stop);
+    if (st == cudaSuccess) return 1;
+    if (st == cudaErrorNotReady) return 0;
+    if (error) *error = cuda_error("cudaEventQuery", st);
+    return -1;
 }
 
 int Plan::run_host(const uint8_t* const* frames, const int32_t* strides, std::string* error) {

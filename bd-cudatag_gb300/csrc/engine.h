@@ -56,6 +56,16 @@ public:
     int submit_host(const uint8_t* const* frames, const int32_t* strides, std::string* error);
     int submit_device(const uint8_t* const* frames, const int32_t* strides, std::string* error);
     int wait(std::string* error);
+    // 1: nothing in flight or finished; 0: running; -1: error.
+    int query(std::string* error);
+
+    // Stream for later submits (a cudaStream_t; null: the plan's own).
+    void set_stream(void* stream);
+
+    // One synchronous device-input run, not graphed, with CUDA events
+    // around every kernel; writes kStageCount stage times (ms).
+    int profile_device(const uint8_t* const* frames, const int32_t* strides, float* stage_ms,
+                       std::string* error);
 
     // Results of the last completed run (host memory).
     const FrameResultHeader* result(int frame) const;

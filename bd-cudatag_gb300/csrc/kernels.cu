@@ -1506,8 +1506,16 @@ __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __r
 
 }  // namespace
 
-void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* io, void* stream_ptr) {
+const char* const kStageNames[kStageCount] = {
+    "stats", "binarize_runs", "merge", "region_stats", "cand_count",
+    "cand_emit", "fit", "decode", "finalize"};
+
+void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* io, void* stream_ptr,
+                      void* const* stage_events) {
     cudaStream_t s = static_cast<cudaStream_t>(stream_ptr);
+    auto mark = [&](int k) {
+        if (stage_events) cudaEventRecord(static_cast<cudaEvent_t>(stage_events[k]), s);
+    };
     const int bands = hd.total_bands;
     int cand_total = 0;
     int dec_total = 0;
@@ -1517,15 +1525,25 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     }
     const int fit_grid = cand_total < 152 * 8 ? cand_total : 152 * 8;
     const int dec_grid = dec_total < 152 * 6 ? dec_total : 152 * 6;
+    mark(0);
     k_stats<<<bands, 256, 0, s>>>(dd, io);
+    mark(1);
     k_binarize_runs<<<bands, 256, 0, s>>>(dd, io);
+    mark(2);
     k_merge<<<bands, 256, 0, s>>>(dd);
+    mark(3);
     k_region_stats<<<bands, 256, 0, s>>>(dd);
+    mark(4);
     k_cand_count<<<bands, 256, 0, s>>>(dd);
+    mark(5);
     k_cand_emit<<<bands, 256, 0, s>>>(dd);
+    mark(6);
     k_fit<<<fit_grid > 0 ? fit_grid : 1, kFitThreads, 0, s>>>(dd, io);
+    mark(7);
     k_decode<<<dec_grid > 0 ? dec_grid : 1, kDecodeThreads, 0, s>>>(dd, io);
+    mark(8);
     k_finalize<<<hd.frames * 2, kFinalThreads, 0, s>>>(dd);
+    mark(9);
 }
 
 }  // namespace bdgb

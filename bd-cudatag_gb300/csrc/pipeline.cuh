@@ -112,8 +112,12 @@ BDGB_HD inline size_t result_bytes(int max_detections) {
 }
 
 // Launch sequence of one batch on one stream (kernels.cu).  `io` is a
-// device array of FrameIO, one per frame.
+// device array of FrameIO, one per frame.  When stage_events is not null it
+// holds kStageCount + 1 cudaEvent_t, recorded before the first kernel and
+// after every kernel, so consecutive events bracket one stage.
+constexpr int kStageCount = 9;
+extern const char* const kStageNames[kStageCount];
 void enqueue_pipeline(const BatchDesc* device_desc, const BatchDesc& host_desc,
-                      const FrameIO* device_io, void* stream);
+                      const FrameIO* device_io, void* stream, void* const* stage_events = nullptr);
 
 }  // namespace bdgb

@@ -1,0 +1,399 @@
+"""Benchmark: batched AprilTag detection on one GB300 versus plain per-frame detect.
+
+Workload (one step = one batch): 4 cameras x 1280x800 uint8 frames, both tag
+families per frame, from 600 seeded synthetic frames (6 tag36h11 + 2 tag16h5
+per frame, side 20-200 px, noise sigma 6, 3x3 blur on odd frames, two decoys
+on every fourth frame, glyph clutter past the candidate cap on every eighth).
+The 600 distinct frames (614 MB) are larger than L2, so no flush is needed.
+
+value     frames/s of the batched path with frames resident in HBM
+          (bd_batch_submit_device), several batches in flight on S streams,
+          timed with CUDA events; p50/p99 = per-batch latency, submit to
+          results on the host.
+e2e       the same through the host-input C ABI (bd_batch_submit_host) with
+          frames in pinned host memory: H2D of the frames and D2H of the result
+          records inside the timed region.
+plain     the reference-style plain path: bd_detector_detect_host per frame
+          and family (two detectors per frame, like two reference detectors).
+roofline  the dominant kernel's algorithmic bytes / CUDA-event duration vs
+          the measured HBM copy bandwidth.
+cpu_baseline  the CPU oracle (a restatement of the reference pipeline; the
+          reference has no CPU detector) on the host cores, bounded sample.
+
+--impl reference times the reference pipeline on the host CPU (the oracle
+port, all host threads), same metric and workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path[:0] = [str(REPO / "bd-cudatag_gb300"), str(REPO / "oracle")]
+
+METRIC = "batched frames/s & p99 ms at 1280x800 vs plain per-frame detect, same GB300"
+W, H = 1280, 800
+POOL = 600
+BATCH = 4
+FAMILIES = 3  # both families
+WORKLOAD = ("config2: 4-camera batches of 1280x800 uint8 frames, tag36h11+tag16h5 decoded per "
+            "frame, 600 seeded frames (6 tag36h11 + 2 tag16h5, side 20-200 px, sigma 6, blur on "
+            "odd frames, decoys on i%4==3, glyph clutter past the candidate cap on i%8==5)")
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def render_pool(count: int, offset: int = 0):
+    import scenes
+
+    frames, truth = scenes.render_many(2, [(W, H)] * count, threads=os.cpu_count() or 8,
+                                       base=scenes.base_seed(2) + offset)
+    return frames, truth
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = REPO / "_work" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        self.path.parent.mkdir(exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.25)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pct(values, q):
+    return float(np.percentile(np.asarray(values), q)) if len(values) else None
+
+
+def run_batched(plans, streams, frame_sets, steps, warmup, device: bool):
+    """Round-robin batches over the plans; returns (elapsed ms by CUDA
+    events, per-batch latencies in ms)."""
+    import torch
+
+    S = len(plans)
+    issued = {}  # plan index -> submit time
+
+    def drain(i, lat):
+        if i in issued:
+            plans[i].wait(copy=False)
+            if lat is not None:
+                lat.append((time.perf_counter() - issued[i]) * 1e3)
+            del issued[i]
+
+    def loop(n, lat, offset):
+        for k in range(n):
+            i = k % S
+            if i in issued:
+                # Poll every plan in flight so completions are stamped when
+                # they happen, not when their slot is reused.
+                while not plans[i].query():
+                    for j in list(issued):
+                        if j != i and plans[j].query():
+                            drain(j, lat)
+                drain(i, lat)
+            frames = frame_sets[(offset + k) % len(frame_sets)]
+            issued[i] = time.perf_counter()
+            plans[i].submit(frames, [W] * BATCH, device=device)
+        for i in list(issued):
+            while not plans[i].query():
+                pass
+            drain(i, lat)
+
+    loop(warmup, None, 0)
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    lat: list[float] = []
+    main = torch.cuda.current_stream()
+    start.record(main)
+    for st in streams:
+        st.wait_event(start)
+    loop(steps, lat, warmup)
+    for st in streams:
+        main.wait_stream(st)
+    stop.record(main)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop), lat
+
+
+def measure_plain(frames, count):
+    import bdcudatag
+
+    dets = [bdcudatag.Detector(f, W, H) for f in (0, 1)]
+    for k in range(5):
+        for d in dets:
+            d.detect(frames[k % len(frames)])
+    lat = []
+    t0 = time.perf_counter()
+    for k in range(count):
+        t = time.perf_counter()
+        for d in dets:
+            d.detect(frames[k % len(frames)])
+        lat.append((time.perf_counter() - t) * 1e3)
+    total = time.perf_counter() - t0
+    gpu_ms = sum(d.stats().average_gpu_ms for d in dets)
+    return {"value": count / total, "unit": "frames/s", "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+            "gpu_ms_per_frame": gpu_ms, "path": "bd_detector_detect_host, one tag36h11 and one "
+            "tag16h5 detector per frame, pageable host frames, CUDA graph"}
+
+
+def measure_roofline(plan, frame_sets, peaks):
+    """Per-stage CUDA-event times over several batches; the dominant stage's
+    algorithmic bytes per launch / its mean duration."""
+    sums = None
+    n = 0
+    for k in range(min(16, len(frame_sets))):
+        st = plan.profile_device(frame_sets[k], [W] * BATCH)
+        if k < 2:
+            continue  # warm-up
+        sums = {s: sums.get(s, 0.0) + v for s, v in st.items()} if sums else dict(st)
+        n += 1
+    mean = {s: v / n for s, v in sums.items()}
+    total = sum(mean.values())
+    dom = max(mean, key=mean.get)
+    T = ((W + 7) // 8) * ((H + 7) // 8)
+    # Algorithmic bytes per frame of each HBM-facing stage.
+    per_frame = {
+        "stats": W * H + 2 * T,                      # frame read once, tile min/max written
+        "binarize_runs": W * H + ((W + 31) // 32) * 4 * H,  # frame band read, bit rows written
+    }
+    stage_bytes = per_frame.get(dom, W * H) * BATCH
+    achieved = stage_bytes / (mean[dom] * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs")
+    return {
+        "bound": "hbm", "kernel": f"k_{dom}", "achieved": round(achieved, 2), "peak": peak,
+        "unit": "GB/s", "frac": round(achieved / peak, 5) if peak else None,
+        "frac_of": "measured copy bandwidth (MEASURED_PEAKS.json)",
+        "bytes_per_launch": stage_bytes, "mean_launch_ms": round(mean[dom], 5),
+        "traffic": None,
+        "stage_ms": {k: round(v, 5) for k, v in mean.items()},
+        "stage_share": {k: round(v / total, 4) for k, v in mean.items()},
+    }
+
+
+def measure_cpu_baseline(frames, seconds_budget=12.0):
+    import oracle
+
+    cores = os.cpu_count() or 1
+    sample = frames[:min(len(frames), 64)]
+    t0 = time.perf_counter()
+    oracle.detect_many(sample[:2], [FAMILIES] * 2, threads=1)  # warm
+    n1 = 4
+    t = time.perf_counter()
+    oracle.detect_many(sample[:n1], [FAMILIES] * n1, threads=1)
+    single = n1 / (time.perf_counter() - t)
+    n = min(len(sample), max(cores * 2, int(seconds_budget * 0.5 * single * cores)))
+    t = time.perf_counter()
+    oracle.detect_many(sample[:n], [FAMILIES] * n, threads=cores)
+    multi = n / (time.perf_counter() - t)
+    return {"value": round(multi, 2), "unit": "frames/s", "cores": cores, "kind": "port",
+            "single_thread": round(single, 2),
+            "sample": f"{n} config2 1280x800 frames, both families, oracle on {cores} threads "
+                      f"(and {n1} frames on 1 thread); {time.perf_counter() - t0:.1f} s of CPU time"}
+
+
+def bench_reference(args, rank):
+    """The reference pipeline on the host CPU (oracle port, all threads)."""
+    import oracle
+
+    if rank != 0:
+        return
+    frames, _ = render_pool(64)
+    cores = os.cpu_count() or 1
+    step_frames = BATCH
+    for k in range(args.warmup):
+        oracle.detect_many(frames[(k * step_frames) % 64:][:step_frames], [FAMILIES] * step_frames,
+                           threads=cores)
+    times = []
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        sl = [frames[(k * step_frames + i) % 64] for i in range(step_frames)]
+        t = time.perf_counter()
+        oracle.detect_many(sl, [FAMILIES] * step_frames, threads=cores)
+        times.append((time.perf_counter() - t) * 1e3)
+    total = time.perf_counter() - t0
+    value = args.steps * step_frames / total
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total * 1e3 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "p50_ms": pct(times, 50), "p99_ms": pct(times, 99),
+        "config": {"workload": WORKLOAD, "batch_frames": step_frames, "frames_pool": 64},
+        "cpu_baseline": {"value": round(value, 2), "unit": "frames/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} steps of {step_frames} config2 frames (both "
+                                   f"families) from 64 seeded frames"},
+        "e2e": {"value": round(value, 2), "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference has no CPU detector; this is the CPU restatement of its pipeline "
+                "(oracle/), run on all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_ours(args, rank, world, local_rank):
+    import torch
+
+    import bdcudatag
+
+    torch.cuda.set_device(local_rank)
+    peaks = {}
+    pk = REPO / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    frames, _ = render_pool(POOL, offset=rank * POOL)
+    pinned = torch.empty((POOL, H, W), dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = np.stack(frames)
+    device = pinned.to(f"cuda:{local_rank}")
+    torch.cuda.synchronize()
+    sets_dev = [[device[(k * BATCH + i) % POOL] for i in range(BATCH)] for k in range(POOL // BATCH)]
+    sets_host = [[pinned[(k * BATCH + i) % POOL] for i in range(BATCH)] for k in range(POOL // BATCH)]
+
+    cams = [(W, H, FAMILIES)] * BATCH
+    plans = [bdcudatag.Batch(cams) for _ in range(args.streams)]
+    streams = [torch.cuda.Stream() for _ in range(args.streams)]
+    for p, s in zip(plans, streams):
+        p.set_stream(s)
+
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(local_rank) as clocks:
+        elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps, args.warmup, device=True)
+    e2e_ms, e2e_lat = run_batched(plans, streams, sets_host, args.steps, args.warmup, device=False)
+    if world > 1:
+        t = torch.tensor([elapsed_ms, e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms, e2e_ms = float(t[0]), float(t[1])
+    frames_total = args.steps * BATCH * world
+    value = frames_total / (elapsed_ms * 1e-3)
+    e2e_value = frames_total / (e2e_ms * 1e-3)
+    if rank != 0:
+        return
+
+    # Correctness spot check against the CPU oracle on one batch.
+    import oracle
+
+    found, out = plans[0].detect(sets_host[0], [W] * BATCH)
+    for i in range(BATCH):
+        for fam in (0, 1):
+            n, want = oracle.Frame(frames[i], fam).detections()
+            assert found[i, fam] == n and out[i, fam, :n].tobytes() == want.tobytes(), "parity"
+
+    for p in plans:
+        p.set_stream(None)
+    roof = measure_roofline(plans[0], sets_dev, peaks)
+    plain = measure_plain(frames, args.plain_frames)
+    cpu = measure_cpu_baseline(frames)
+    result_bytes = BATCH * ((32 + 2 * plans[0].max_detections * 84 + 255) // 256 * 256)
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(elapsed_ms / args.steps, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic",
+        "p50_ms": round(pct(lat, 50), 4), "p99_ms": round(pct(lat, 99), 4),
+        "config": {"workload": WORKLOAD, "batch_frames": BATCH, "streams": args.streams,
+                   "frames_pool": POOL, "families_per_frame": 2,
+                   "l2": "inputs larger than L2 (600 distinct 1 MB frames cycled)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e_value, 2), "unit": "frames/s",
+                "p50_ms": round(pct(e2e_lat, 50), 4), "p99_ms": round(pct(e2e_lat, 99), 4),
+                "h2d_bytes_per_step": BATCH * W * H, "d2h_bytes_per_step": result_bytes,
+                "path": "bd_batch_submit_host/bd_batch_wait, frames in pinned host memory"},
+        "plain": plain,
+        "speedup_vs_plain": round(value / plain["value"], 2),
+        "e2e_speedup_vs_plain": round(e2e_value / plain["value"], 2),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "gpu_launches": 9 * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--streams", type=int, default=4)
+    ap.add_argument("--plain-frames", type=int, default=300)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local_rank = dist_info()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        if args.impl == "reference":
+            if rank != 0:
+                return
+        else:
+            torch.cuda.set_device(local_rank)
+            dist.init_process_group("nccl")
+    if args.impl == "reference":
+        bench_reference(args, rank)
+    else:
+        bench_ours(args, rank, world, local_rank)
+    if world > 1 and args.impl != "reference":
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -68,6 +68,25 @@ BD_API int32_t bd_batch_submit_host(bd_batch* batch, const uint8_t* const* frame
 BD_API int32_t bd_batch_submit_device(bd_batch* batch, const uint8_t* const* frames,
                                       const int32_t* strides);
 BD_API int32_t bd_batch_wait(bd_batch* batch, bd_detection* out, int32_t* found);
+/* 1 when no batch is in flight or the one in flight has finished (wait then
+ * returns at once), 0 while it runs, a negative bd_status on error. */
+BD_API int32_t bd_batch_query(bd_batch* batch);
+
+/* Later submits of this batch are enqueued on `cuda_stream` (a
+ * cudaStream_t of the batch's device; NULL: the batch's own stream), so a
+ * caller can order detection after its own work and time it with its own
+ * events.  Several batches on several streams run concurrently. */
+BD_API int32_t bd_batch_set_stream(bd_batch* batch, void* cuda_stream);
+
+/* Pipeline stages, in launch order (for bd_batch_profile_device). */
+BD_API int32_t bd_stage_count(void);
+BD_API const char* bd_stage_name(int32_t stage);
+
+/* Runs one device-input batch synchronously without the CUDA graph, with
+ * CUDA events between kernels, and writes each stage's time in ms to
+ * stage_ms[bd_stage_count()].  Results are as for bd_batch_detect_device. */
+BD_API int32_t bd_batch_profile_device(bd_batch* batch, const uint8_t* const* frames,
+                                       const int32_t* strides, float* stage_ms);
 
 /* Pinned host staging buffer of camera i (width * height bytes, stride =
  * width).  A frame written here is submitted without the staging copy by

@@ -219,3 +219,33 @@ def test_batch_matches_single_frames():
         for fam in (0, 1):
             if found[i, fam] > 0:
                 same_records(out2[i, fam, :found[i, fam]], out[i, fam, :found[i, fam]])
+
+
+def test_batch_pinned_stream_query_profile():
+    torch = pytest.importorskip("torch")
+    sizes = [(1280, 800)] * 4
+    frames, _ = scenes.render_many(2, sizes, threads=8)
+    pinned = torch.empty((4, 800, 1280), dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = np.stack(frames)
+    batch = bdcudatag.Batch([(1280, 800, 3)] * 4)
+    found, out = batch.detect(frames)  # pageable: staged copy
+    f2, o2 = batch.detect([pinned[i] for i in range(4)], strides=[1280] * 4)  # pinned: direct DMA
+    assert np.array_equal(found, f2) and np.array_equal(out.view(np.uint8), o2.view(np.uint8))
+    stream = torch.cuda.Stream()
+    batch.set_stream(stream)
+    batch.submit([pinned[i] for i in range(4)], strides=[1280] * 4)
+    stream.synchronize()
+    assert batch.query()
+    f3, o3 = batch.wait()
+    assert np.array_equal(found, f3) and np.array_equal(out.view(np.uint8), o3.view(np.uint8))
+    batch.set_stream(None)
+    dev = [torch.from_numpy(f).cuda() for f in frames]
+    prof = batch.profile_device(dev, [1280] * 4)
+    assert len(prof) == 9 and all(v >= 0 for v in prof.values())
+    f4, o4 = batch.wait()
+    assert np.array_equal(found, f4)
+    for i in range(4):
+        for fam in (0, 1):
+            n, want = oracle.Frame(frames[i], fam).detections()
+            assert found[i, fam] == n
+            same_records(out[i, fam, :n], want)
