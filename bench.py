@@ -294,13 +294,14 @@ def bench_ours(args, rank, world, local_rank):
     pk = REPO / "MEASURED_PEAKS.json"
     if pk.exists():
         peaks = json.loads(pk.read_text())
-    frames, _ = render_pool(POOL, offset=rank * POOL)
-    pinned = torch.empty((POOL, H, W), dtype=torch.uint8, pin_memory=True)
+    pool = 64 if args.quick else POOL
+    frames, _ = render_pool(pool, offset=rank * POOL)
+    pinned = torch.empty((pool, H, W), dtype=torch.uint8, pin_memory=True)
     pinned.numpy()[:] = np.stack(frames)
     device = pinned.to(f"cuda:{local_rank}")
     torch.cuda.synchronize()
-    sets_dev = [[device[(k * BATCH + i) % POOL] for i in range(BATCH)] for k in range(POOL // BATCH)]
-    sets_host = [[pinned[(k * BATCH + i) % POOL] for i in range(BATCH)] for k in range(POOL // BATCH)]
+    sets_dev = [[device[(k * BATCH + i) % pool] for i in range(BATCH)] for k in range(pool // BATCH)]
+    sets_host = [[pinned[(k * BATCH + i) % pool] for i in range(BATCH)] for k in range(pool // BATCH)]
 
     cams = [(W, H, FAMILIES)] * BATCH
     plans = [bdcudatag.Batch(cams) for _ in range(args.streams)]
@@ -310,6 +311,12 @@ def bench_ours(args, rank, world, local_rank):
 
     if world > 1:
         torch.distributed.barrier()
+    if args.quick:
+        elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps, args.warmup, device=True)
+        if rank == 0:
+            print(json.dumps({"quick": True, "value": args.steps * BATCH / (elapsed_ms * 1e-3),
+                              "unit": "frames/s", "p99_ms": pct(lat, 99)}), flush=True)
+        return
     with ClockSampler(local_rank) as clocks:
         elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps, args.warmup, device=True)
     e2e_ms, e2e_lat = run_batched(plans, streams, sets_host, args.steps, args.warmup, device=False)
@@ -366,11 +373,13 @@ def bench_ours(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--streams", type=int, default=4)
     ap.add_argument("--plain-frames", type=int, default=300)
+    ap.add_argument("--quick", action="store_true",
+                    help="profiling run: 64-frame pool, batched device-input loop only")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local_rank = dist_info()
