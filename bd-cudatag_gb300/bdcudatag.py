@@ -87,7 +87,7 @@ GB300_SYMBOLS = [
     "bd_batch_submit_host", "bd_batch_submit_device", "bd_batch_wait", "bd_batch_host_frame",
     "bd_batch_last_gpu_ms", "bd_batch_counts", "bd_batch_debug_stage", "bd_detector_debug_stage",
     "bd_batch_set_stream", "bd_stage_count", "bd_stage_name", "bd_batch_profile_device",
-    "bd_batch_query",
+    "bd_batch_query", "bd_tile_stats_device_noalloc",
 ]
 
 _LIB = None
@@ -147,6 +147,9 @@ def lib() -> ctypes.CDLL:
         L.bd_stage_name.argtypes = [ctypes.c_int32]
         L.bd_batch_profile_device.argtypes = [_P, _P, _P, _P]
         L.bd_batch_query.argtypes = [_P]
+        L.bd_tile_stats_device_noalloc.argtypes = [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                   _P, _P, _P, _P]
+        L.bd_tile_stats_device_noalloc.restype = ctypes.c_int32
         L.bd_batch_query.restype = ctypes.c_int32
         _LIB = L
     return _LIB

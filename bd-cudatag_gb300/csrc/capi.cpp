@@ -48,6 +48,11 @@ bool config_size_ok(const bd_config* config) {
 
 }  // namespace
 
+namespace bdgb {
+// Lets other translation units (noalloc.cu) report through bd_last_error().
+void set_last_error(const char* message) { set_error(message ? message : ""); }
+}  // namespace bdgb
+
 struct bd_detector {
     bdgb::Plan* plan = nullptr;
     int family = 0;

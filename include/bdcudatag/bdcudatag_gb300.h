@@ -112,6 +112,40 @@ BD_API int64_t bd_batch_debug_stage(bd_batch* batch, int32_t camera, const char*
 BD_API int64_t bd_detector_debug_stage(bd_detector* detector, const char* name, void* dst,
                                        int64_t dst_bytes);
 
+/*
+ * Tile statistics of one frame, for callers that cannot allocate memory.
+ * No counterpart in the reference.
+ *
+ * Who needs it: code that must not call cudaMalloc (or any allocating
+ * routine) when it runs -- a camera or ISP callback that may not block, a
+ * system that fixes its memory at start-up (real-time, safety-certified), a
+ * plugin living inside another framework's allocator.  Detectors and batches
+ * allocate at creation; this entry point allocates nothing ever: it uses the
+ * caller's buffers plus a 2 KiB scratch array compiled into the library,
+ * which every GPU that loads the library holds until the process exits.
+ *
+ * Computes what the first pipeline stage of a detector computes for the
+ * frame gray_device (device memory, rows `stride` bytes apart):
+ *   tile_min_device, tile_max_device: ceil(width/8) * ceil(height/8) bytes
+ *     each, the minimum / maximum of every 8x8 tile, row-major;
+ *   frame_device[0..2]: noise-floor span quartile, Otsu level, ROI tile rows.
+ * All buffers are device memory of the current device; the work is enqueued
+ * on cuda_stream (NULL: the legacy default stream) and the call returns
+ * without waiting.  Frames up to BD_NOALLOC_MAX_WIDTH x BD_NOALLOC_MAX_HEIGHT
+ * are accepted; larger ones return BD_ERROR_INVALID_ARGUMENT.
+ *
+ * The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress); make that first call before capturing a stream.
+ * Every call shares the one scratch array per device and clears it first:
+ * calls whose GPU work overlaps race and must be serialised by the caller.
+ */
+#define BD_NOALLOC_MAX_WIDTH 8192
+#define BD_NOALLOC_MAX_HEIGHT 16384
+BD_API int32_t bd_tile_stats_device_noalloc(const uint8_t* gray_device, int32_t width,
+                                            int32_t height, int32_t stride,
+                                            uint8_t* tile_min_device, uint8_t* tile_max_device,
+                                            uint32_t* frame_device, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
