@@ -182,6 +182,10 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     };
     cudaError_t st = cudaGetDevice(&im.device);
     if (st != cudaSuccess) return fail(cuda_error("cudaGetDevice", st));
+    if (prepare_pipeline() != 0) {
+        cudaGetLastError();
+        return fail("cudaFuncSetAttribute failed");
+    }
 
     const int nf = static_cast<int>(frames.size());
     const int md = config.max_detections;
@@ -199,7 +203,8 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     hd.frames = nf;
     std::vector<size_t> off_frame(nf), off_tmin(nf), off_tmax(nf), off_lo(nf), off_hi(nf),
         off_bits(nf), off_rc(nf), off_runs(nf), off_parent(nf), off_area(nf), off_bbox(nf),
-        off_meta(nf), off_bands(nf), off_cands(nf), off_hull(nf), off_quads(nf), off_dec(nf);
+        off_meta(nf), off_bands(nf), off_cands(nf), off_hull(nf), off_quads(nf), off_dec(nf),
+        off_lroots(nf), off_lcount(nf), off_mode(nf);
     im.frame_offset.resize(nf);
     size_t frame_total = 0;
     for (int i = 0; i < nf; ++i) {
@@ -252,6 +257,9 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
         off_area[i] = carve.take(sizeof(uint32_t) * slots);
         off_bbox[i] = carve.take(sizeof(uint32_t) * 4 * slots);
         off_meta[i] = carve.take(sizeof(uint32_t) * slots);
+        off_lroots[i] = carve.take(sizeof(uint32_t) * slots);
+        off_lcount[i] = carve.take(sizeof(uint32_t) * d.tile_h);
+        off_mode[i] = carve.take(sizeof(uint32_t) * d.tile_h);
         off_bands[i] = carve.take(sizeof(uint32_t) * 64 * d.tile_h);
         off_cands[i] = carve.take(sizeof(uint32_t) * mc);
         off_hull[i] = carve.take(sizeof(float) * 8 * mc);
@@ -288,6 +296,9 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
         d.area = reinterpret_cast<uint32_t*>(base + off_area[i]);
         d.bbox = reinterpret_cast<uint32_t*>(base + off_bbox[i]);
         d.cand_meta = reinterpret_cast<uint32_t*>(base + off_meta[i]);
+        d.lroots = reinterpret_cast<uint32_t*>(base + off_lroots[i]);
+        d.lroot_count = reinterpret_cast<uint32_t*>(base + off_lcount[i]);
+        d.band_mode = reinterpret_cast<uint32_t*>(base + off_mode[i]);
         d.band_bins = reinterpret_cast<uint32_t*>(base + off_bands[i]);
         d.candidates = reinterpret_cast<uint32_t*>(base + off_cands[i]);
         d.state = im.states + i;

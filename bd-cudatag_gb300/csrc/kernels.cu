@@ -297,14 +297,63 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
 }
 
 // ===========================================================================
-// 2. Pooled threshold, binarization of the row band and run extraction for
-//    one band of 8 rows; warp w owns row y0 + w.
+// 2. Pooled threshold, binarization of the row band, run extraction and the
+//    band-local connected components, for one band of 8 rows; warp w owns
+//    row y0 + w.
+//
+//    The runs of a band are unioned in shared memory (same-row fragments and
+//    8-connected runs of consecutive rows inside the band), and area / bbox
+//    are aggregated per band-local root with shared-memory atomics.  Global
+//    memory then receives one parent link per run (to its band-local root)
+//    and one aggregate per band-local root; k_merge only unions across band
+//    boundaries and k_region_stats folds band roots into global roots.  The
+//    local root is the band's smallest slot of the component, so every root
+//    is still the component's smallest slot id (reference invariant,
+//    gpu_detector.cu:398-421).  A band with more than kLocalCap runs falls
+//    back to one root per run and full merging in k_merge.
 // ===========================================================================
+constexpr int kLocalCap = 2048;
+constexpr size_t kBandSmemBytes = 6 * kLocalCap * sizeof(uint32_t);
+
+__device__ __forceinline__ uint32_t s_find(uint32_t* par, uint32_t x) {
+    for (;;) {
+        const uint32_t p = par[x];
+        if (p == x) return x;
+        const uint32_t gp = par[p];
+        par[x] = gp;
+        x = gp;
+    }
+}
+
+__device__ __forceinline__ void s_union(uint32_t* par, uint32_t a, uint32_t b) {
+    a = s_find(par, a);
+    b = s_find(par, b);
+    while (a != b) {
+        if (a > b) {
+            const uint32_t t = a;
+            a = b;
+            b = t;
+        }
+        const uint32_t old = atomicMin(&par[b], a);
+        if (old == a) break;
+        b = s_find(par, old);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restrict__ b,
                                                        const FrameIO* __restrict__ io) {
+    extern __shared__ __align__(16) uint32_t s_dyn[];
+    uint32_t* sm_run = s_dyn;
+    uint32_t* sm_par = s_dyn + kLocalCap;
+    uint32_t* sm_area = s_dyn + 2 * kLocalCap;
+    uint32_t* sm_minx = s_dyn + 3 * kLocalCap;
+    uint32_t* sm_maxx = s_dyn + 4 * kLocalCap;
+    uint32_t* sm_rows = s_dyn + 5 * kLocalCap;
     __shared__ uint8_t s_thresh[BD_MAX_WIDTH / kTile];
     __shared__ uint32_t s_bits[kTile][BD_MAX_WIDTH / 32];
-    __shared__ uint32_t s_runs;
+    __shared__ uint32_t s_rowtot[kTile];
+    __shared__ uint32_t s_rowoff[kTile + 1];
+    __shared__ uint32_t s_nroots;
 
     const int tid = threadIdx.x;
     const int fi = frame_of_band(b, blockIdx.x);
@@ -314,6 +363,8 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
     const int W = d.width, H = d.height, tw = d.tile_w, th = d.tile_h, words = d.words;
     const int y0 = ty * kTile;
     const int rows = min(kTile, H - y0);
+    const uint32_t row_cap = static_cast<uint32_t>(d.row_cap);
+    const uint32_t band_base = static_cast<uint32_t>(y0) * row_cap;
 
     const int top = th - static_cast<int>(st->top_enc);
     const int bottom = static_cast<int>(st->bottom_enc) - 1;
@@ -323,9 +374,12 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
             d.bits[static_cast<int64_t>(y0 + i / words) * words + i % words] = 0xffffffffu;
         }
         if (tid < rows) d.row_count[y0 + tid] = 0;
+        if (tid == 0) {
+            d.lroot_count[ty] = 0;
+            d.band_mode[ty] = 0;
+        }
         return;
     }
-    if (tid == 0) s_runs = 0;
 
     // Row band: contrasting tiles +- 4, or the whole row (reference :345-355).
     const int lo = d.row_lo[ty], hi = d.row_hi[ty];
@@ -354,12 +408,17 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
         if (mx - mn >= floor_contrast) thr = (mn + mx + 1) >> 1;
         s_thresh[t] = static_cast<uint8_t>(thr);
     }
+    if (tid < kTile) s_rowtot[tid] = 0;
     __syncthreads();
 
     const int w = tid >> 5, lane = tid & 31;
     const uint8_t* gray = io[fi].gray;
     const int64_t stride = io[fi].stride;
     const bool vec = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 15u) == 0;
+    const int per = (words + 31) >> 5;
+    const int c0 = lane * per;
+    const int c1 = min(c0 + per, words);
+    uint32_t first_index = 0;  // exclusive prefix of this lane's fragments in its row
     if (w < rows) {
         const int y = y0 + w;
         const uint8_t* row = gray + static_cast<int64_t>(y) * stride;
@@ -390,12 +449,7 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
             s_bits[w][wx] = m;
         }
         __syncwarp();
-
-        // Runs of black pixels; a run restarts at every 32-pixel word and
-        // k_merge rejoins the pieces (reference k_find_runs :427-504).
-        const int per = (words + 31) >> 5;
-        const int c0 = lane * per;
-        const int c1 = min(c0 + per, words);
+        // Fragments per lane, then the row's prefix (reference :448-470).
         uint32_t cnt = 0;
         for (int c = c0; c < c1; ++c) {
             const uint32_t m = s_bits[w][c];
@@ -406,10 +460,34 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
             const uint32_t n = __shfl_up_sync(kFull, incl, off);
             if (lane >= off) incl += n;
         }
+        first_index = incl - cnt;
         const uint32_t total = __shfl_sync(kFull, incl, 31);
-        const uint32_t row_cap = static_cast<uint32_t>(d.row_cap);
-        uint32_t index = incl - cnt;
+        if (lane == 0) {
+            const uint32_t kept = min(total, row_cap);
+            d.row_count[y] = kept;
+            s_rowtot[w] = kept;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t off = 0;
+        for (int r = 0; r < kTile; ++r) {
+            s_rowoff[r] = off;
+            off += s_rowtot[r];
+        }
+        s_rowoff[kTile] = off;
+        s_nroots = 0;
+        atomicAdd(&st->counts[2], off);
+    }
+    __syncthreads();
+    const uint32_t band_total = s_rowoff[kTile];
+    const bool local = band_total <= static_cast<uint32_t>(kLocalCap);
+
+    // Emit the runs (reference :472-503).
+    if (w < rows) {
+        const int y = y0 + w;
         const uint32_t slot_base = static_cast<uint32_t>(y) * row_cap;
+        uint32_t index = first_index;
         for (int c = c0; c < c1; ++c) {
             const uint32_t m = s_bits[w][c];
             uint32_t starts = ~m & ((m << 1) | 1u);
@@ -424,27 +502,116 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
                     e = min(e, last);
                     const int x1 = (c << 5) + e;
                     const uint32_t id = slot_base + index;
-                    d.runs[id] = (static_cast<uint32_t>(x0) & 0xffffu) | (static_cast<uint32_t>(x1) << 16);
-                    d.parent[id] = id;
-                    d.area[id] = 0;
-                    reinterpret_cast<uint4*>(d.bbox)[id] = make_uint4(kNone, kNone, 0u, 0u);
+                    const uint32_t packed = (static_cast<uint32_t>(x0) & 0xffffu) | (static_cast<uint32_t>(x1) << 16);
+                    d.runs[id] = packed;
+                    if (local) {
+                        const uint32_t li = s_rowoff[w] + index;
+                        sm_run[li] = packed;
+                        sm_par[li] = li;
+                    } else {
+                        // Fallback: every run is its own band root.
+                        d.parent[id] = id;
+                        d.area[id] = static_cast<uint32_t>(x1 - x0 + 1);
+                        reinterpret_cast<uint4*>(d.bbox)[id] = make_uint4(x0, y, x1, y);
+                        d.lroots[band_base + s_rowoff[w] + index] = id;
+                    }
                 }
                 ++index;
             }
         }
-        if (lane == 0) {
-            const uint32_t kept = min(total, row_cap);
-            d.row_count[y] = kept;
-            atomicAdd(&s_runs, kept);
+    }
+    if (!local) {
+        if (tid == 0) {
+            d.lroot_count[ty] = band_total;
+            d.band_mode[ty] = 1;
+        }
+        return;
+    }
+    for (uint32_t i = tid; i < band_total; i += blockDim.x) {
+        sm_area[i] = 0u;
+        sm_minx[i] = 0xffffffffu;
+        sm_maxx[i] = 0u;
+        sm_rows[i] = 0u;
+    }
+    __syncthreads();
+
+    // Band-local unions (the reference's k_merge_runs rules inside the band).
+    if (w < rows) {
+        const uint32_t n = s_rowtot[w];
+        const uint32_t base = s_rowoff[w];
+        const uint32_t prev_n = w > 0 ? s_rowtot[w - 1] : 0u;
+        const uint32_t pbase = w > 0 ? s_rowoff[w - 1] : 0u;
+        for (uint32_t i = lane; i < n; i += 32) {
+            const uint32_t run = sm_run[base + i];
+            const int x0 = static_cast<int>(run & 0xffffu);
+            const int x1 = static_cast<int>(run >> 16);
+            if (i > 0) {
+                const int px1 = static_cast<int>(sm_run[base + i - 1] >> 16);
+                if (px1 + 1 >= x0) s_union(sm_par, base + i, base + i - 1);
+            }
+            if (prev_n == 0) continue;
+            int lo2 = 0, hi2 = static_cast<int>(prev_n) - 1, first = static_cast<int>(prev_n);
+            while (lo2 <= hi2) {
+                const int mid = (lo2 + hi2) >> 1;
+                if (static_cast<int>(sm_run[pbase + mid] >> 16) >= x0 - 1) {
+                    first = mid;
+                    hi2 = mid - 1;
+                } else {
+                    lo2 = mid + 1;
+                }
+            }
+            for (int k = first; k < static_cast<int>(prev_n); ++k) {
+                const int px0 = static_cast<int>(sm_run[pbase + k] & 0xffffu);
+                if (px0 > x1 + 1) break;
+                s_union(sm_par, base + i, pbase + k);
+            }
         }
     }
     __syncthreads();
-    if (tid == 0 && s_runs) atomicAdd(&st->counts[2], s_runs);
+
+    // Band-local roots and their area / bbox.
+    for (uint32_t i = tid; i < band_total; i += blockDim.x) {
+        uint32_t r = i;
+        while (sm_par[r] != r) r = sm_par[r];
+        int row = 0;
+        while (row + 1 < kTile && s_rowoff[row + 1] <= i) ++row;
+        const uint32_t run = sm_run[i];
+        const uint32_t x0 = run & 0xffffu, x1 = run >> 16;
+        atomicAdd(&sm_area[r], x1 - x0 + 1);
+        atomicMin(&sm_minx[r], x0);
+        atomicMax(&sm_maxx[r], x1);
+        atomicOr(&sm_rows[r], 1u << row);
+        // parent link = the local root's slot
+        int rrow = 0;
+        while (rrow + 1 < kTile && s_rowoff[rrow + 1] <= r) ++rrow;
+        const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (i - s_rowoff[row]);
+        const uint32_t rslot = static_cast<uint32_t>(y0 + rrow) * row_cap + (r - s_rowoff[rrow]);
+        d.parent[slot] = rslot;
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < band_total; i += blockDim.x) {
+        if (sm_par[i] != i) continue;
+        int row = 0;
+        while (row + 1 < kTile && s_rowoff[row + 1] <= i) ++row;
+        const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (i - s_rowoff[row]);
+        const uint32_t rm = sm_rows[i];
+        d.area[slot] = sm_area[i];
+        reinterpret_cast<uint4*>(d.bbox)[slot] =
+            make_uint4(sm_minx[i], static_cast<uint32_t>(y0 + __ffs(rm) - 1), sm_maxx[i],
+                       static_cast<uint32_t>(y0 + 31 - __clz(rm)));
+        d.lroots[band_base + atomicAdd(&s_nroots, 1u)] = slot;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        d.lroot_count[ty] = s_nroots;
+        d.band_mode[ty] = 0;
+    }
 }
 
 // ===========================================================================
-// 3. Union of same-row fragments and 8-connected runs of the row above
-//    (reference k_merge_runs :509-557).
+// 3. Unions across band boundaries: the first row of a band against the last
+//    row of the band above; every row of a fallback band (the reference's
+//    k_merge_runs :509-557 rules).
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b) {
     const int fi = frame_of_band(b, blockIdx.x);
@@ -453,6 +620,8 @@ __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b) 
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int y = ty * kTile + w;
     if (y <= 0 || y >= d.height) return;
+    const bool full = d.band_mode[ty] != 0;
+    if (!full && w != 0) return;
     const int n = static_cast<int>(d.row_count[y]);
     if (n == 0) return;
     const int row_cap = d.row_cap;
@@ -466,7 +635,7 @@ __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b) 
         const uint32_t run = cur[i];
         const int x0 = static_cast<int>(run & 0xffffu);
         const int x1 = static_cast<int>(run >> 16);
-        if (i > 0) {
+        if (full && i > 0) {
             const int px1 = static_cast<int>(cur[i - 1] >> 16);
             if (px1 + 1 >= x0) uf_union(parent, cur_base + i, cur_base + i - 1);
         }
@@ -490,27 +659,26 @@ __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b) 
 }
 
 // ===========================================================================
-// 4. Area and bounding box per root (reference k_region_stats :562-586).
+// 4. Area and bounding box per global root: each band root adds its
+//    aggregate to its global root (reference k_region_stats :562-586 sums the
+//    same quantities run by run).
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_region_stats(const BatchDesc* __restrict__ b) {
     const int fi = frame_of_band(b, blockIdx.x);
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int y = ty * kTile + w;
-    if (y >= d.height) return;
-    const int n = static_cast<int>(d.row_count[y]);
-    const uint32_t base = static_cast<uint32_t>(y * d.row_cap);
-    for (int i = lane; i < n; i += 32) {
-        const uint32_t idx = base + static_cast<uint32_t>(i);
-        const uint32_t root = uf_find(d.parent, idx);
-        const uint32_t run = d.runs[idx];
-        const uint32_t x0 = run & 0xffffu, x1 = run >> 16;
-        atomicAdd(&d.area[root], x1 - x0 + 1);
-        atomicMin(&d.bbox[root * 4 + 0], x0);
-        atomicMin(&d.bbox[root * 4 + 1], static_cast<uint32_t>(y));
-        atomicMax(&d.bbox[root * 4 + 2], x1);
-        atomicMax(&d.bbox[root * 4 + 3], static_cast<uint32_t>(y));
+    const uint32_t n = d.lroot_count[ty];
+    const uint32_t* list = d.lroots + static_cast<int64_t>(ty) * kTile * d.row_cap;
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const uint32_t s = list[k];
+        const uint32_t g = uf_find(d.parent, s);
+        if (g == s) continue;
+        const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[s];
+        atomicAdd(&d.area[g], d.area[s]);
+        atomicMin(&d.bbox[g * 4 + 0], bb.x);
+        atomicMin(&d.bbox[g * 4 + 1], bb.y);
+        atomicMax(&d.bbox[g * 4 + 2], bb.z);
+        atomicMax(&d.bbox[g * 4 + 3], bb.w);
     }
 }
 
@@ -672,91 +840,123 @@ __device__ __forceinline__ uint32_t pack_point(int x, int y) {
     return (static_cast<uint32_t>(x) & 0xffffu) | (static_cast<uint32_t>(y) << 16);
 }
 
-__device__ bool hull_to_quad(const uint32_t* hull, int count, float quad[4][2]) {
-    if (count < 4 || count > kMaxHullVertices) return false;
-    float vx[kFitDirections];
-    float vy[kFitDirections];
-    if (count > kFitDirections) return false;
-    for (int i = 0; i < count; ++i) {
-        vx[i] = static_cast<float>(hull[i] & 0xffffu);
-        vy[i] = static_cast<float>(hull[i] >> 16);
-    }
+// hull_to_quad (reference :736-831) run by one warp: lane i holds hull
+// vertex i; each round drops the vertex whose triangle with its neighbours
+// has the smallest area (first index on ties, as the reference's strict <),
+// found with a warp arg-min instead of a serial scan.  The remaining checks
+// run on lane 0 with the reference's expressions.  Returns the result in all
+// lanes.
+__device__ bool hull_to_quad_warp(const uint32_t* hull, int count, float quad[4][2], int lane) {
+    if (count < 4 || count > kMaxHullVertices || count > 32) return false;
+    float vx = lane < count ? static_cast<float>(hull[lane] & 0xffffu) : 0.0f;
+    float vy = lane < count ? static_cast<float>(hull[lane] >> 16) : 0.0f;
     while (count > 4) {
-        int best = -1;
-        float best_area = FLT_MAX;
-        for (int i = 0; i < count; ++i) {
-            const int prev = (i + count - 1) % count;
-            const int next = (i + 1) % count;
-            const float ax = vx[i] - vx[prev];
-            const float ay = vy[i] - vy[prev];
-            const float bx = vx[next] - vx[i];
-            const float by = vy[next] - vy[i];
-            const float area = fabsf(ax * by - ay * bx) * 0.5f;
-            if (area < best_area) {
-                best_area = area;
-                best = i;
+        const int prev = (lane + count - 1) % count;
+        const int next = (lane + 1) % count;
+        const float pvx = __shfl_sync(kFull, vx, prev), pvy = __shfl_sync(kFull, vy, prev);
+        const float nvx = __shfl_sync(kFull, vx, next), nvy = __shfl_sync(kFull, vy, next);
+        float area = FLT_MAX;
+        if (lane < count) {
+            const float ax = vx - pvx;
+            const float ay = vy - pvy;
+            const float bx = nvx - vx;
+            const float by = nvy - vy;
+            area = fabsf(ax * by - ay * bx) * 0.5f;
+            if (!(area < FLT_MAX)) area = FLT_MAX;
+        }
+        int idx = lane < count ? lane : 64;
+        float best_area = area;
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oa = __shfl_xor_sync(kFull, best_area, off);
+            const int oi = __shfl_xor_sync(kFull, idx, off);
+            if (oa < best_area || (oa == best_area && oi < idx)) {
+                best_area = oa;
+                idx = oi;
             }
         }
-        if (best < 0) return false;
-        for (int i = best; i + 1 < count; ++i) {
-            vx[i] = vx[i + 1];
-            vy[i] = vy[i + 1];
+        if (!(best_area < FLT_MAX)) return false;
+        const float sx = __shfl_down_sync(kFull, vx, 1), sy = __shfl_down_sync(kFull, vy, 1);
+        if (lane >= idx) {
+            vx = sx;
+            vy = sy;
         }
         --count;
     }
-    float area2 = 0.0f;
+    float qx[4], qy[4];
     for (int i = 0; i < 4; ++i) {
-        const int j = (i + 1) & 3;
-        area2 += vx[i] * vy[j] - vx[j] * vy[i];
+        qx[i] = __shfl_sync(kFull, vx, i);
+        qy[i] = __shfl_sync(kFull, vy, i);
     }
-    if (fabsf(area2) < 24.0f) return false;
-    if (area2 < 0.0f) {
-        for (int i = 0; i < 2; ++i) {
-            const float tx = vx[i + 1], ty = vy[i + 1];
-            vx[i + 1] = vx[3 - i];
-            vy[i + 1] = vy[3 - i];
-            vx[3 - i] = tx;
-            vy[3 - i] = ty;
+    int ok = 0;
+    if (lane == 0) {
+        float* x = qx;
+        float* y = qy;
+        ok = 1;
+        float area2 = 0.0f;
+        for (int i = 0; i < 4; ++i) {
+            const int j = (i + 1) & 3;
+            area2 += x[i] * y[j] - x[j] * y[i];
+        }
+        if (fabsf(area2) < 24.0f) ok = 0;
+        if (ok && area2 < 0.0f) {
+            for (int i = 0; i < 2; ++i) {
+                const float tx = x[i + 1], tyy = y[i + 1];
+                x[i + 1] = x[3 - i];
+                y[i + 1] = y[3 - i];
+                x[3 - i] = tx;
+                y[3 - i] = tyy;
+            }
+        }
+        float min_side = FLT_MAX, max_side = 0.0f;
+        for (int i = 0; ok && i < 4; ++i) {
+            const int j = (i + 1) & 3;
+            const float ex = x[j] - x[i];
+            const float ey = y[j] - y[i];
+            const float len = sqrtf(ex * ex + ey * ey);
+            if (len < 4.0f) {
+                ok = 0;
+                break;
+            }
+            min_side = fminf(min_side, len);
+            max_side = fmaxf(max_side, len);
+            const int p = (i + 3) & 3;
+            const float ax = x[i] - x[p];
+            const float ay = y[i] - y[p];
+            const float bx = x[j] - x[i];
+            const float by = y[j] - y[i];
+            if (ax * by - ay * bx <= 0.0f) {
+                ok = 0;
+                break;
+            }
+            const float dot = ax * bx + ay * by;
+            const float n1 = sqrtf(ax * ax + ay * ay);
+            const float n2 = sqrtf(bx * bx + by * by);
+            if (n1 < 1e-3f || n2 < 1e-3f || fabsf(dot / (n1 * n2)) > 0.97f) {
+                ok = 0;
+                break;
+            }
+        }
+        if (ok && max_side > 12.0f * min_side) ok = 0;
+        if (ok) {
+            const float cx = 0.25f * (x[0] + x[1] + x[2] + x[3]);
+            const float cy = 0.25f * (y[0] + y[1] + y[2] + y[3]);
+            for (int i = 0; i < 4; ++i) {
+                const float dx = x[i] - cx;
+                const float dy = y[i] - cy;
+                const float len = sqrtf(dx * dx + dy * dy);
+                if (len > 1e-3f) {
+                    x[i] += dx / len * 0.65f;
+                    y[i] += dy / len * 0.65f;
+                }
+            }
         }
     }
-    float min_side = FLT_MAX, max_side = 0.0f;
+    ok = __shfl_sync(kFull, ok, 0);
     for (int i = 0; i < 4; ++i) {
-        const int j = (i + 1) & 3;
-        const float ex = vx[j] - vx[i];
-        const float ey = vy[j] - vy[i];
-        const float len = sqrtf(ex * ex + ey * ey);
-        if (len < 4.0f) return false;
-        min_side = fminf(min_side, len);
-        max_side = fmaxf(max_side, len);
-        const int p = (i + 3) & 3;
-        const float ax = vx[i] - vx[p];
-        const float ay = vy[i] - vy[p];
-        const float bx = vx[j] - vx[i];
-        const float by = vy[j] - vy[i];
-        if (ax * by - ay * bx <= 0.0f) return false;
-        const float dot = ax * bx + ay * by;
-        const float n1 = sqrtf(ax * ax + ay * ay);
-        const float n2 = sqrtf(bx * bx + by * by);
-        if (n1 < 1e-3f || n2 < 1e-3f) return false;
-        if (fabsf(dot / (n1 * n2)) > 0.97f) return false;
+        quad[i][0] = __shfl_sync(kFull, qx[i], 0);
+        quad[i][1] = __shfl_sync(kFull, qy[i], 0);
     }
-    if (max_side > 12.0f * min_side) return false;
-    const float cx = 0.25f * (vx[0] + vx[1] + vx[2] + vx[3]);
-    const float cy = 0.25f * (vy[0] + vy[1] + vy[2] + vy[3]);
-    for (int i = 0; i < 4; ++i) {
-        const float dx = vx[i] - cx;
-        const float dy = vy[i] - cy;
-        const float len = sqrtf(dx * dx + dy * dy);
-        if (len > 1e-3f) {
-            vx[i] += dx / len * 0.65f;
-            vy[i] += dy / len * 0.65f;
-        }
-    }
-    for (int i = 0; i < 4; ++i) {
-        quad[i][0] = vx[i];
-        quad[i][1] = vy[i];
-    }
-    return true;
+    return ok != 0;
 }
 
 __device__ __forceinline__ float sample_bilinear(const uint8_t* image, int width, int height,
@@ -788,21 +988,43 @@ __device__ __forceinline__ bool intersect_lines(const float li[4], const float l
     return true;
 }
 
-__device__ __forceinline__ float directional_rise(const uint8_t* image, int width, int height,
-                                                  int64_t stride, float x, float y, float dx,
-                                                  float dy) {
-    const float ahead = sample_bilinear(image, width, height, stride, x + dx * 0.7f, y + dy * 0.7f);
-    const float behind = sample_bilinear(image, width, height, stride, x - dx * 0.7f, y - dy * 0.7f);
+// One warp fits one edge (reference fit_edge_line_warp :881-1016).  Sample
+// s (< 16) along the edge is probed by lanes s and s + 16, which take the
+// even and odd probe steps and leave the profile in shared memory; lane s
+// then picks the peak exactly as the reference lane does.  The moments sit
+// in lanes 0..15 (zero above), so the shuffle tree sums them in the
+// reference's order.
+__device__ __forceinline__ float sample_ro(const uint8_t* __restrict__ image, int width, int height,
+                                           int64_t stride, float x, float y) {
+    if (!(x >= 0.0f && y >= 0.0f && x < static_cast<float>(width - 1) &&
+          y < static_cast<float>(height - 1))) {
+        return -1.0f;
+    }
+    const int ix = static_cast<int>(x);
+    const int iy = static_cast<int>(y);
+    const float fx = x - static_cast<float>(ix);
+    const float fy = y - static_cast<float>(iy);
+    const uint8_t* p = image + static_cast<int64_t>(iy) * stride + ix;
+    const float a = __ldg(p);
+    const float bb = __ldg(p + 1);
+    const float c = __ldg(p + stride);
+    const float dd = __ldg(p + stride + 1);
+    return (a * (1.0f - fx) + bb * fx) * (1.0f - fy) + (c * (1.0f - fx) + dd * fx) * fy;
+}
+
+__device__ __forceinline__ float rise_ro(const uint8_t* __restrict__ image, int width, int height,
+                                         int64_t stride, float x, float y, float dx, float dy) {
+    const float ahead = sample_ro(image, width, height, stride, x + dx * 0.7f, y + dy * 0.7f);
+    const float behind = sample_ro(image, width, height, stride, x - dx * 0.7f, y - dy * 0.7f);
     if (ahead < 0.0f || behind < 0.0f) return 0.0f;
     return ahead - behind;
 }
 
-// One warp fits one edge: lanes < samples probe across the edge, moments
-// are reduced with the shuffle tree, lane 0 turns them into a line
-// (reference fit_edge_line_warp :881-1016).
-__device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8_t* image, int width,
-                                   int height, int64_t stride, int dim, bool first_pass, int lane,
-                                   float line[4]) {
+constexpr int kMaxProbes = kFitProbeHalf * 2 + 1;
+
+__device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8_t* __restrict__ image,
+                                   int width, int height, int64_t stride, int dim, bool first_pass,
+                                   int lane, float* s_mags, float line[4]) {
     const int bi = (edge + 1) & 3;
     const float ax = quad[edge][0], ay = quad[edge][1];
     const float bx = quad[bi][0], by = quad[bi][1];
@@ -820,20 +1042,30 @@ __device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8
     const float step = range / static_cast<float>(half);
     const int samples = min(max(static_cast<int>(len / 6.0f), 8), 16);
 
+    const int sample = lane & 15;
+    const int parity = lane >> 4;
+    float px = 0.0f, py = 0.0f;
+    if (sample < samples) {
+        const float alpha = static_cast<float>(sample + 1) / static_cast<float>(samples + 1);
+        px = ax + alpha * ex;
+        py = ay + alpha * ey;
+        float* mags = s_mags + sample * kMaxProbes;
+#pragma unroll 4
+        for (int i = parity; i < probes; i += 2) {
+            const float t = step * static_cast<float>(i - half);
+            mags[i] = rise_ro(image, width, height, stride, px + nx * t, py + ny * t, nx, ny);
+        }
+    }
+    __syncwarp();
+
     float mx = 0.0f, my = 0.0f, mxx = 0.0f, mxy = 0.0f, myy = 0.0f;
     int used = 0;
-    if (lane < samples) {
-        const float alpha = static_cast<float>(lane + 1) / static_cast<float>(samples + 1);
-        const float px = ax + alpha * ex;
-        const float py = ay + alpha * ey;
-        float mags[kFitProbeHalf * 2 + 1];
+    if (parity == 0 && sample < samples) {
+        const float* mags = s_mags + sample * kMaxProbes;
         float best_mag = 0.0f;
         int best = -1;
         for (int i = 0; i < probes; ++i) {
-            const float t = step * static_cast<float>(i - half);
-            const float mag = directional_rise(image, width, height, stride, px + nx * t,
-                                               py + ny * t, nx, ny);
-            mags[i] = mag;
+            const float mag = mags[i];
             if (mag > best_mag) {
                 best_mag = mag;
                 best = i;
@@ -855,10 +1087,10 @@ __device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8
         if (best >= 0 && best_mag >= 6.0f) {
             float t = step * static_cast<float>(best - half);
             if (best > 0 && best < probes - 1) {
-                const float m0 = directional_rise(image, width, height, stride, px + nx * (t - step),
-                                                  py + ny * (t - step), nx, ny);
-                const float m2 = directional_rise(image, width, height, stride, px + nx * (t + step),
-                                                  py + ny * (t + step), nx, ny);
+                const float m0 = rise_ro(image, width, height, stride, px + nx * (t - step),
+                                         py + ny * (t - step), nx, ny);
+                const float m2 = rise_ro(image, width, height, stride, px + nx * (t + step),
+                                         py + ny * (t + step), nx, ny);
                 const float den = m0 - 2.0f * best_mag + m2;
                 if (den < -1e-3f) t += fminf(fmaxf(0.5f * (m0 - m2) / den, -0.5f), 0.5f) * step;
             }
@@ -880,6 +1112,7 @@ __device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8
         myy += __shfl_down_sync(kFull, myy, off);
         used += __shfl_down_sync(kFull, used, off);
     }
+    __syncwarp();
     if (lane != 0) return true;
     if (used < 4) return false;
     const float inv = 1.0f / static_cast<float>(used);
@@ -946,25 +1179,31 @@ __device__ float apply_refined_lines(float quad[4][2], const float lines[4][4], 
     return moved;
 }
 
-constexpr int kFitThreads = 128;
+constexpr int kFitThreads = 256;
 constexpr int kFitWarps = kFitThreads / 32;
 
 // Flattened (frame, candidate) work list: CTA c takes items c, c + grid, ...
+// The hull is built once per candidate; warps 0-3 refine the quad for the
+// frame's first requested family and warps 4-7 for the second, concurrently.
 __global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict__ b,
                                                      const FrameIO* __restrict__ io) {
     __shared__ uint32_t boundary[2 * kMaxBoundaryRows];
     __shared__ float probe_dot[kFitWarps][kFitDirections];
     __shared__ uint32_t probe_point[kFitWarps][kFitDirections];
     __shared__ uint32_t extreme[kFitDirections];
+    __shared__ uint32_t s_hull[kFitDirections];
+    __shared__ int s_hc;
     __shared__ float hull_quad[4][2];
-    __shared__ float fit_quad[4][2];
-    __shared__ float edge_lines[4][4];
-    __shared__ int edge_have[4];
+    __shared__ float fit_quad[2][4][2];
+    __shared__ float edge_lines[2][4][4];
+    __shared__ int edge_have[2][4];
     __shared__ int quad_ok;
-    __shared__ float refine_moved;
+    __shared__ int s_done[2];
+    __shared__ float s_mags[kFitWarps][16 * kMaxProbes];
     __shared__ int s_prefix[kMaxFrames + 1];
 
     const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         int run = 0;
         for (int f = 0; f < b->frames; ++f) {
@@ -975,8 +1214,8 @@ __global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict
     }
     __syncthreads();
     const int total = s_prefix[b->frames];
-    const int dir = tid & 31;
-    const int part = tid >> 5;
+    const int dir = lane;
+    const int part = warp;
     float ux, uy;
     {
         const float angle =
@@ -990,7 +1229,7 @@ __global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict
         const FrameDesc& d = b->f[fi];
         const int ci = item - s_prefix[fi];
         const int mc = d.max_candidates;
-        const uint8_t* gray = io[fi].gray;
+        const uint8_t* __restrict__ gray = io[fi].gray;
         const int64_t stride = io[fi].stride;
         const uint32_t root = d.candidates[ci];
         const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[root];
@@ -1032,7 +1271,8 @@ __global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict
         }
         __syncthreads();
 
-        // Extreme boundary point per direction; the first point wins ties.
+        // Extreme boundary point per direction; the first point wins ties
+        // (reference :1134-1170, eight parts instead of four: same result).
         const int chunk = (points + kFitWarps - 1) / kFitWarps;
         const int begin = part * chunk;
         const int end = min(points, begin + chunk);
@@ -1062,73 +1302,94 @@ __global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict
             extreme[tid] = point;
         }
         __syncthreads();
-
-        float* hull_out = d.hull_quads + static_cast<int64_t>(ci) * 8;
         if (tid == 0) {
-            uint32_t hull[kFitDirections];
             int hc = 0;
             for (int i = 0; i < kFitDirections; ++i) {
                 const uint32_t p = extreme[i];
                 if (p == kNone) continue;
-                if (hc > 0 && hull[hc - 1] == p) continue;
-                hull[hc++] = p;
+                if (hc > 0 && s_hull[hc - 1] == p) continue;
+                s_hull[hc++] = p;
             }
-            while (hc > 1 && hull[0] == hull[hc - 1]) --hc;
-            float quad[4][2];
-            const bool ok = hull_to_quad(hull, hc, quad);
-            quad_ok = ok ? 1 : 0;
-            const float nan = bdmath::quiet_nan();
-            for (int i = 0; i < 4; ++i) {
-                hull_quad[i][0] = quad[i][0];
-                hull_quad[i][1] = quad[i][1];
-                hull_out[i * 2 + 0] = ok ? quad[i][0] : nan;
-                hull_out[i * 2 + 1] = ok ? quad[i][1] : nan;
-            }
-            if (ok) atomicAdd(&d.state->counts[3], 1u);
+            while (hc > 1 && s_hull[0] == s_hull[hc - 1]) --hc;
+            s_hc = hc;
         }
         __syncthreads();
 
-        const int warp = tid >> 5, lane = tid & 31;
-        for (int fam = 0; fam < 2; ++fam) {
-            if (!(d.families & (1u << fam))) continue;
-            float* out = d.quads + (static_cast<int64_t>(fam) * mc + ci) * 8;
-            if (!quad_ok) {
-                if (tid < 8) out[tid] = bdmath::quiet_nan();
-                continue;
+        float* hull_out = d.hull_quads + static_cast<int64_t>(ci) * 8;
+        if (warp == 0) {
+            float quad[4][2] = {};
+            const bool ok = hull_to_quad_warp(s_hull, s_hc, quad, lane);
+            if (lane < 8) {
+                const float v = quad[lane >> 1][lane & 1];
+                hull_quad[lane >> 1][lane & 1] = v;
+                fit_quad[0][lane >> 1][lane & 1] = v;
+                fit_quad[1][lane >> 1][lane & 1] = v;
+                hull_out[lane] = ok ? v : bdmath::quiet_nan();
             }
-            if (tid < 8) fit_quad[tid >> 1][tid & 1] = hull_quad[tid >> 1][tid & 1];
-            __syncthreads();
-            if (d.refine_edges) {
-                for (int iteration = 0; iteration < kFitIterations; ++iteration) {
-                    float line[4];
-                    const bool ok = fit_edge_line_warp(fit_quad, warp, gray, d.width, d.height, stride,
-                                                       family_dim(fam), iteration == 0, lane, line);
-                    if (lane == 0) {
-                        edge_have[warp] = ok ? 1 : 0;
-                        if (ok) {
-                            for (int k = 0; k < 4; ++k) edge_lines[warp][k] = line[k];
-                        }
-                    }
-                    __syncthreads();
-                    if (tid == 0) {
-                        float quad[4][2];
-                        for (int i = 0; i < 4; ++i) {
-                            quad[i][0] = fit_quad[i][0];
-                            quad[i][1] = fit_quad[i][1];
-                        }
-                        refine_moved = apply_refined_lines(quad, edge_lines, edge_have);
-                        for (int i = 0; i < 4; ++i) {
-                            fit_quad[i][0] = quad[i][0];
-                            fit_quad[i][1] = quad[i][1];
-                        }
-                    }
-                    __syncthreads();
-                    if (refine_moved < 0.15f) break;
-                }
+            if (lane == 0) {
+                quad_ok = ok ? 1 : 0;
+                if (ok) atomicAdd(&d.state->counts[3], 1u);
             }
-            if (tid < 8) out[tid] = fit_quad[tid >> 1][tid & 1];
-            __syncthreads();
         }
+        __syncthreads();
+
+        // Families of this frame: slot 0 = lowest requested family.
+        const uint32_t fams = d.families & 3u;
+        const int nfam = __popc(fams);
+        const int fam_of_slot[2] = {(fams & 1u) ? 0 : 1, 1};
+        if (!quad_ok) {
+            if (tid < 8 * nfam) {
+                const int fam = fam_of_slot[tid >> 3];
+                d.quads[(static_cast<int64_t>(fam) * mc + ci) * 8 + (tid & 7)] = bdmath::quiet_nan();
+            }
+            __syncthreads();
+            continue;
+        }
+        if (d.refine_edges) {
+            const int slot = warp >> 2;
+            const int edge = warp & 3;
+            const bool mine = slot < nfam;
+            const int dim = family_dim(fam_of_slot[slot < nfam ? slot : 0]);
+            if (tid < 2) s_done[tid] = 0;
+            __syncthreads();
+            for (int iteration = 0; iteration < kFitIterations; ++iteration) {
+                if (mine && !s_done[slot]) {
+                    float line[4];
+                    const bool ok = fit_edge_line_warp(fit_quad[slot], edge, gray, d.width, d.height,
+                                                       stride, dim, iteration == 0, lane, s_mags[warp],
+                                                       line);
+                    if (lane == 0) {
+                        edge_have[slot][edge] = ok ? 1 : 0;
+                        if (ok) {
+                            for (int k = 0; k < 4; ++k) edge_lines[slot][edge][k] = line[k];
+                        }
+                    }
+                }
+                __syncthreads();
+                if (lane == 0 && edge == 0 && mine && !s_done[slot]) {
+                    float quad[4][2];
+                    for (int i = 0; i < 4; ++i) {
+                        quad[i][0] = fit_quad[slot][i][0];
+                        quad[i][1] = fit_quad[slot][i][1];
+                    }
+                    const float moved = apply_refined_lines(quad, edge_lines[slot], edge_have[slot]);
+                    for (int i = 0; i < 4; ++i) {
+                        fit_quad[slot][i][0] = quad[i][0];
+                        fit_quad[slot][i][1] = quad[i][1];
+                    }
+                    // Converged quads skip the second pass (reference :1229-1231).
+                    if (moved < 0.15f) s_done[slot] = 1;
+                }
+                __syncthreads();
+            }
+        }
+        if (tid < 8 * nfam) {
+            const int slot = tid >> 3;
+            const int fam = fam_of_slot[slot];
+            d.quads[(static_cast<int64_t>(fam) * mc + ci) * 8 + (tid & 7)] =
+                fit_quad[slot][(tid & 7) >> 1][tid & 1];
+        }
+        __syncthreads();
     }
 }
 
@@ -1506,6 +1767,12 @@ __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __r
 
 }  // namespace
 
+int prepare_pipeline() {
+    // Shared memory beyond 48 KB per block needs an opt-in, per device.
+    return cudaFuncSetAttribute(k_binarize_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(kBandSmemBytes)) == cudaSuccess ? 0 : -1;
+}
+
 const char* const kStageNames[kStageCount] = {
     "stats", "binarize_runs", "merge", "region_stats", "cand_count",
     "cand_emit", "fit", "decode", "finalize"};
@@ -1528,7 +1795,7 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     mark(0);
     k_stats<<<bands, 256, 0, s>>>(dd, io);
     mark(1);
-    k_binarize_runs<<<bands, 256, 0, s>>>(dd, io);
+    k_binarize_runs<<<bands, 256, kBandSmemBytes, s>>>(dd, io);
     mark(2);
     k_merge<<<bands, 256, 0, s>>>(dd);
     mark(3);

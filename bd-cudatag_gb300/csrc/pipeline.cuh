@@ -87,6 +87,9 @@ struct FrameDesc {
     uint32_t* area;                // slots (valid at roots)
     uint32_t* bbox;                // 4 * slots (valid at roots)
     uint32_t* cand_meta;           // slots: bin << 24 | rank in band, or kNone
+    uint32_t* lroots;              // slots: per band (at its first slot) the band-local roots
+    uint32_t* lroot_count;         // tile_h: band-local roots per band
+    uint32_t* band_mode;           // tile_h: 0 band-local unions done, 1 fallback (one root per run)
     uint32_t* band_bins;           // tile_h * 64 candidate counts, then exclusive prefixes
     uint32_t* candidates;          // max_candidates root slots, canonical order
     FrameState* state;
@@ -116,6 +119,9 @@ BDGB_HD inline size_t result_bytes(int max_detections) {
 // holds kStageCount + 1 cudaEvent_t, recorded before the first kernel and
 // after every kernel, so consecutive events bracket one stage.
 constexpr int kStageCount = 9;
+// Per-device kernel attributes; call with the device current before the
+// first enqueue.  0 on success.
+int prepare_pipeline();
 extern const char* const kStageNames[kStageCount];
 void enqueue_pipeline(const BatchDesc* device_desc, const BatchDesc& host_desc,
                       const FrameIO* device_io, void* stream, void* const* stage_events = nullptr);
