@@ -545,7 +545,9 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
             const uint32_t run = sm_run[base + i];
             const int x0 = static_cast<int>(run & 0xffffu);
             const int x1 = static_cast<int>(run >> 16);
-            if (i > 0) {
+            // Row 0 of the frame is never merged, not even its word-split
+            // fragments (reference k_merge_runs :514 returns for y <= 0).
+            if (i > 0 && y0 + w > 0) {
                 const int px1 = static_cast<int>(sm_run[base + i - 1] >> 16);
                 if (px1 + 1 >= x0) s_union(sm_par, base + i, base + i - 1);
             }
