@@ -866,17 +866,11 @@ __device__ bool hull_to_quad_warp(const uint32_t* hull, int count, float quad[4]
             area = fabsf(ax * by - ay * bx) * 0.5f;
             if (!(area < FLT_MAX)) area = FLT_MAX;
         }
-        int idx = lane < count ? lane : 64;
-        float best_area = area;
-        for (int off = 16; off > 0; off >>= 1) {
-            const float oa = __shfl_xor_sync(kFull, best_area, off);
-            const int oi = __shfl_xor_sync(kFull, idx, off);
-            if (oa < best_area || (oa == best_area && oi < idx)) {
-                best_area = oa;
-                idx = oi;
-            }
-        }
-        if (!(best_area < FLT_MAX)) return false;
+        // Areas are >= 0, so their bit patterns order like the values.
+        const uint32_t key = __float_as_uint(area);
+        const uint32_t best_key = __reduce_min_sync(kFull, key);
+        if (best_key == __float_as_uint(FLT_MAX)) return false;
+        const int idx = __ffs(__ballot_sync(kFull, lane < count && key == best_key)) - 1;
         const float sx = __shfl_down_sync(kFull, vx, 1), sy = __shfl_down_sync(kFull, vy, 1);
         if (lane >= idx) {
             vx = sx;
@@ -996,22 +990,28 @@ __device__ __forceinline__ bool intersect_lines(const float li[4], const float l
 // then picks the peak exactly as the reference lane does.  The moments sit
 // in lanes 0..15 (zero above), so the shuffle tree sums them in the
 // reference's order.
+// Bilinear sample with the reference's bounds rule (sample_bilinear
+// :833-849): -1 outside [0, width-1) x [0, height-1).  The address is
+// clamped and the result selected instead of branching, so the loads of
+// consecutive probes can be in flight together; in-range values are computed
+// with the reference's expression.
 __device__ __forceinline__ float sample_ro(const uint8_t* __restrict__ image, int width, int height,
                                            int64_t stride, float x, float y) {
-    if (!(x >= 0.0f && y >= 0.0f && x < static_cast<float>(width - 1) &&
-          y < static_cast<float>(height - 1))) {
-        return -1.0f;
-    }
-    const int ix = static_cast<int>(x);
-    const int iy = static_cast<int>(y);
-    const float fx = x - static_cast<float>(ix);
-    const float fy = y - static_cast<float>(iy);
+    const bool in = x >= 0.0f && y >= 0.0f && x < static_cast<float>(width - 1) &&
+                    y < static_cast<float>(height - 1);
+    const float xc = in ? x : 0.0f;
+    const float yc = in ? y : 0.0f;
+    const int ix = static_cast<int>(xc);
+    const int iy = static_cast<int>(yc);
+    const float fx = xc - static_cast<float>(ix);
+    const float fy = yc - static_cast<float>(iy);
     const uint8_t* p = image + static_cast<int64_t>(iy) * stride + ix;
     const float a = __ldg(p);
     const float bb = __ldg(p + 1);
     const float c = __ldg(p + stride);
     const float dd = __ldg(p + stride + 1);
-    return (a * (1.0f - fx) + bb * fx) * (1.0f - fy) + (c * (1.0f - fx) + dd * fx) * fy;
+    const float v = (a * (1.0f - fx) + bb * fx) * (1.0f - fy) + (c * (1.0f - fx) + dd * fx) * fy;
+    return in ? v : -1.0f;
 }
 
 __device__ __forceinline__ float rise_ro(const uint8_t* __restrict__ image, int width, int height,
@@ -1052,7 +1052,7 @@ __device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8
         px = ax + alpha * ex;
         py = ay + alpha * ey;
         float* mags = s_mags + sample * kMaxProbes;
-#pragma unroll 4
+#pragma unroll 8
         for (int i = parity; i < probes; i += 2) {
             const float t = step * static_cast<float>(i - half);
             mags[i] = rise_ro(image, width, height, stride, px + nx * t, py + ny * t, nx, ny);
@@ -1257,16 +1257,33 @@ __global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict
                     lo = mid + 1;
                 }
             }
-            const uint32_t base = static_cast<uint32_t>(y * d.row_cap);
+            const uint32_t* row_label = d.parent + static_cast<int64_t>(y) * d.row_cap;
             int left = -1, right = -1;
-            for (int k = first; k < n; ++k) {
-                const uint32_t run = row_runs[k];
-                const int rx0 = static_cast<int>(run & 0xffffu);
-                const int rx1 = static_cast<int>(run >> 16);
-                if (rx0 > x1) break;
-                if (d.parent[base + static_cast<uint32_t>(k)] != root) continue;
-                left = left < 0 ? rx0 : min(left, rx0);
-                right = right < 0 ? rx1 : max(right, rx1);
+            // In order from `first`, stopping at the first run past the
+            // bbox; four runs and labels are loaded ahead of the checks.
+            for (int k = first; k < n; k += 4) {
+                uint32_t rr[4], lab[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int kk = min(k + j, n - 1);
+                    rr[j] = row_runs[kk];
+                    lab[j] = row_label[kk];
+                }
+                bool stop = false;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (stop || k + j >= n) continue;
+                    const int rx0 = static_cast<int>(rr[j] & 0xffffu);
+                    const int rx1 = static_cast<int>(rr[j] >> 16);
+                    if (rx0 > x1) {
+                        stop = true;
+                        continue;
+                    }
+                    if (lab[j] != root) continue;
+                    left = left < 0 ? rx0 : min(left, rx0);
+                    right = right < 0 ? rx1 : max(right, rx1);
+                }
+                if (stop) break;
             }
             boundary[2 * s] = left < 0 ? kNone : pack_point(left, y);
             boundary[2 * s + 1] = right < 0 ? kNone : pack_point(right, y);
