@@ -63,6 +63,13 @@ class Detection(ctypes.Structure):
     ]
 
 
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("rejected", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("mean_batch_frames", ctypes.c_double), ("plans", ctypes.c_int32),
+                ("peak_inflight", ctypes.c_int32), ("device_bytes", ctypes.c_int64)]
+
+
 class Camera(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32),
                 ("families", ctypes.c_uint32), ("reserved", ctypes.c_int32)]
@@ -88,6 +95,8 @@ GB300_SYMBOLS = [
     "bd_batch_last_gpu_ms", "bd_batch_counts", "bd_batch_debug_stage", "bd_detector_debug_stage",
     "bd_batch_set_stream", "bd_stage_count", "bd_stage_name", "bd_batch_profile_device",
     "bd_batch_query", "bd_tile_stats_device_noalloc",
+    "bd_server_create", "bd_server_destroy", "bd_server_submit", "bd_server_wait",
+    "bd_server_poll", "bd_server_get_stats",
 ]
 
 _LIB = None
@@ -150,6 +159,16 @@ def lib() -> ctypes.CDLL:
         L.bd_tile_stats_device_noalloc.argtypes = [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                    _P, _P, _P, _P]
         L.bd_tile_stats_device_noalloc.restype = ctypes.c_int32
+        L.bd_server_create.argtypes = [_P, ctypes.c_int32, ctypes.POINTER(Config), ctypes.c_int64,
+                                       ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+        L.bd_server_create.restype = _P
+        L.bd_server_destroy.argtypes = [_P]
+        L.bd_server_submit.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int32]
+        L.bd_server_submit.restype = ctypes.c_int64
+        for n in ("bd_server_wait", "bd_server_poll"):
+            getattr(L, n).argtypes = [_P, ctypes.c_int64, _P, _P, ctypes.POINTER(ctypes.c_double)]
+            getattr(L, n).restype = ctypes.c_int32
+        L.bd_server_get_stats.argtypes = [_P, ctypes.POINTER(ServerStats)]
         L.bd_batch_query.restype = ctypes.c_int32
         _LIB = L
     return _LIB
@@ -334,6 +353,52 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "handle", None):
             lib().bd_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+
+class Server:
+    """Continuous-batching server over several cameras (bd_server)."""
+
+    def __init__(self, cameras: list[tuple[int, int, int]], config: Config | None = None,
+                 device_budget: int = 8 << 30, max_batches: int = 4, queue_depth: int = 8):
+        arr = (Camera * len(cameras))(*[Camera(w, h, fam, 0) for w, h, fam in cameras])
+        status = ctypes.c_int32(0)
+        cfg = config if config is not None else default_config()
+        self.handle = lib().bd_server_create(ctypes.cast(arr, _P), len(cameras), ctypes.byref(cfg),
+                                             device_budget, max_batches, queue_depth,
+                                             ctypes.byref(status))
+        if not self.handle:
+            raise RuntimeError(f"bd_server_create failed ({status.value}): {last_error()}")
+        self.cameras = list(cameras)
+        self.max_detections = min(max(cfg.max_detections, 1), 256)
+
+    def submit(self, camera: int, frame, stride: int | None = None) -> int:
+        s = stride if stride is not None else self.cameras[camera][0]
+        t = lib().bd_server_submit(self.handle, camera, _ptr(frame), s)
+        return int(t)
+
+    def wait(self, ticket: int, block: bool = True):
+        """(status, found[2], detections[2, max_detections], latency_ms)."""
+        out = np.zeros((2, self.max_detections), dtype=DETECTION_DTYPE)
+        found = np.zeros(2, dtype=np.int32)
+        lat = ctypes.c_double(0.0)
+        fn = lib().bd_server_wait if block else lib().bd_server_poll
+        rc = fn(self.handle, ticket, out.ctypes.data, found.ctypes.data, ctypes.byref(lat))
+        if rc < 0:
+            raise RuntimeError(f"server wait failed ({rc}): {last_error()}")
+        return rc, found, out, lat.value
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        lib().bd_server_get_stats(self.handle, ctypes.byref(st))
+        return st
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().bd_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

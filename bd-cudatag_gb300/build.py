@@ -30,7 +30,7 @@ SCENES_LIB = PKG / "libbdscenes.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu"]
-CXX_SOURCES = ["capi.cpp"]
+CXX_SOURCES = ["capi.cpp", "server.cpp"]
 
 
 def nvcc() -> str:

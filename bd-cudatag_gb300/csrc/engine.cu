@@ -440,6 +440,50 @@ int Plan::submit_device(const uint8_t* const* frames, const int32_t* strides, st
     return 0;
 }
 
+int Plan::submit_slots(const uint8_t* const* frames, const int32_t* strides, std::string* error) {
+    Impl& im = *impl_;
+    if (im.pending) {
+        if (error) *error = "a batch is already in flight";
+        return -1;
+    }
+    const cudaStream_t s = im.active();
+    cudaEventRecord(im.ev_start, s);
+    for (int i = 0; i < this->frames(); ++i) {
+        const int w = frames_[i].width, h = frames_[i].height;
+        uint8_t* dev = im.frames_dev + im.frame_offset[i];
+        if (!frames[i]) {
+            im.io_staging[i].gray = nullptr;
+            im.io_staging[i].stride = 0;
+            continue;
+        }
+        cudaPointerAttributes attr;
+        const bool pinned = cudaPointerGetAttributes(&attr, frames[i]) == cudaSuccess &&
+                            attr.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        if (pinned) {
+            cudaMemcpy2DAsync(dev, w, frames[i], strides[i], w, h, cudaMemcpyHostToDevice, s);
+        } else {
+            uint8_t* stage = im.frames_pinned + im.frame_offset[i];
+            for (int y = 0; y < h; ++y) {
+                std::memcpy(stage + static_cast<size_t>(y) * w,
+                            frames[i] + static_cast<size_t>(y) * strides[i], w);
+            }
+            cudaMemcpyAsync(dev, stage, static_cast<size_t>(w) * h, cudaMemcpyHostToDevice, s);
+        }
+        im.io_staging[i].gray = dev;
+        im.io_staging[i].stride = w;
+    }
+    im.launch(2, s);
+    cudaEventRecord(im.ev_stop, s);
+    const cudaError_t st = cudaGetLastError();
+    if (st != cudaSuccess) {
+        if (error) *error = cuda_error("cudaGraphLaunch", st);
+        return -1;
+    }
+    im.pending = true;
+    return 0;
+}
+
 void Plan::set_stream(void* stream) {
     impl_->user_stream = static_cast<cudaStream_t>(stream);
 }

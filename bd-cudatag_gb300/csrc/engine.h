@@ -59,6 +59,12 @@ public:
     // 1: nothing in flight or finished; 0: running; -1: error.
     int query(std::string* error);
 
+    // Batch with some slots unused: frames[i] == nullptr leaves slot i out
+    // of this launch (its kernels return at once and it reports nothing).
+    // Host frames (page-locked or not) are copied to the plan's device
+    // buffers; results as for submit_host.
+    int submit_slots(const uint8_t* const* frames, const int32_t* strides, std::string* error);
+
     // Stream for later submits (a cudaStream_t; null: the plan's own).
     void set_stream(void* stream);
 

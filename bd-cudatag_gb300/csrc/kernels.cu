@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
 
     const int tid = threadIdx.x;
     const int fi = frame_of_band(b, blockIdx.x);
+    if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
     FrameState* st = d.state;
@@ -357,6 +358,7 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
 
     const int tid = threadIdx.x;
     const int fi = frame_of_band(b, blockIdx.x);
+    if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
     FrameState* st = d.state;
@@ -615,8 +617,10 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
 //    row of the band above; every row of a fallback band (the reference's
 //    k_merge_runs :509-557 rules).
 // ===========================================================================
-__global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b) {
+__global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b,
+                                               const FrameIO* __restrict__ io) {
     const int fi = frame_of_band(b, blockIdx.x);
+    if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -665,8 +669,10 @@ __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b) 
 //    aggregate to its global root (reference k_region_stats :562-586 sums the
 //    same quantities run by run).
 // ===========================================================================
-__global__ void __launch_bounds__(256) k_region_stats(const BatchDesc* __restrict__ b) {
+__global__ void __launch_bounds__(256) k_region_stats(const BatchDesc* __restrict__ b,
+                                                      const FrameIO* __restrict__ io) {
     const int fi = frame_of_band(b, blockIdx.x);
+    if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
     const uint32_t n = d.lroot_count[ty];
@@ -707,7 +713,8 @@ __device__ __forceinline__ int candidate_bin(const FrameDesc& d, uint32_t idx) {
     return 63 - min(log2_area, 63);
 }
 
-__global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict__ b) {
+__global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict__ b,
+                                                    const FrameIO* __restrict__ io) {
     __shared__ uint32_t s_rowbin[kTile][64];
     __shared__ uint32_t s_chunk[32][64];
     __shared__ uint32_t s_total[64];
@@ -715,6 +722,7 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
 
     const int tid = threadIdx.x;
     const int fi = frame_of_band(b, blockIdx.x);
+    if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
     FrameState* st = d.state;
@@ -814,8 +822,10 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
 // ===========================================================================
 // 6. Ordered flattening (reference k_order_candidates :642-654).
 // ===========================================================================
-__global__ void __launch_bounds__(256) k_cand_emit(const BatchDesc* __restrict__ b) {
+__global__ void __launch_bounds__(256) k_cand_emit(const BatchDesc* __restrict__ b,
+                                                   const FrameIO* __restrict__ io) {
     const int fi = frame_of_band(b, blockIdx.x);
+    if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
     const FrameState* st = d.state;
@@ -1816,13 +1826,13 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     mark(1);
     k_binarize_runs<<<bands, 256, kBandSmemBytes, s>>>(dd, io);
     mark(2);
-    k_merge<<<bands, 256, 0, s>>>(dd);
+    k_merge<<<bands, 256, 0, s>>>(dd, io);
     mark(3);
-    k_region_stats<<<bands, 256, 0, s>>>(dd);
+    k_region_stats<<<bands, 256, 0, s>>>(dd, io);
     mark(4);
-    k_cand_count<<<bands, 256, 0, s>>>(dd);
+    k_cand_count<<<bands, 256, 0, s>>>(dd, io);
     mark(5);
-    k_cand_emit<<<bands, 256, 0, s>>>(dd);
+    k_cand_emit<<<bands, 256, 0, s>>>(dd, io);
     mark(6);
     k_fit<<<fit_grid > 0 ? fit_grid : 1, kFitThreads, 0, s>>>(dd, io);
     mark(7);

@@ -113,6 +113,52 @@ BD_API int64_t bd_detector_debug_stage(bd_detector* detector, const char* name, 
                                        int64_t dst_bytes);
 
 /*
+ * Continuous-batching server.  No counterpart in the reference.
+ *
+ * Frames of several cameras are submitted at any time; a scheduler thread
+ * launches a batch whenever one of its preallocated batch plans is free,
+ * taking the oldest waiting frame of every camera (cameras with nothing
+ * waiting sit that launch out), so frames that arrive while batches run join
+ * the next launch and up to `plans` batches overlap on the GPU.  Plans are
+ * created at bd_server_create, as many as device_budget_bytes holds (at most
+ * max_batches): that is the admission limit.  Each result equals what a
+ * bd_detector of the camera's size and family returns for the frame.
+ *
+ * bd_server_submit returns a ticket (>= 0), or BD_ERROR_OUT_OF_MEMORY when
+ * the camera already has queue_depth frames waiting or running.  A frame in
+ * page-locked host memory is read in place (keep it unchanged until its
+ * ticket completes); other frames are copied at submit.  bd_server_wait /
+ * bd_server_poll return 1 with the results (out: 2 * max_detections records,
+ * family-major; found[2], -1 for a family the camera does not decode;
+ * latency_ms from submit to results), 0 from poll while pending, or a
+ * negative bd_status.  A ticket is collected once.
+ */
+typedef struct bd_server bd_server;
+
+typedef struct bd_server_stats {
+    uint64_t submitted;
+    uint64_t completed;
+    uint64_t rejected;
+    uint64_t batches;
+    double mean_batch_frames;
+    int32_t plans;
+    int32_t peak_inflight;
+    int64_t device_bytes;
+} bd_server_stats;
+
+BD_API bd_server* bd_server_create(const bd_camera* cameras, int32_t count, const bd_config* config,
+                                   int64_t device_budget_bytes, int32_t max_batches,
+                                   int32_t queue_depth, int32_t* status_out);
+BD_API void bd_server_destroy(bd_server* server);
+BD_API int64_t bd_server_submit(bd_server* server, int32_t camera, const uint8_t* gray,
+                                int32_t stride);
+BD_API int32_t bd_server_wait(bd_server* server, int64_t ticket, bd_detection* out, int32_t* found,
+                              double* latency_ms);
+BD_API int32_t bd_server_poll(bd_server* server, int64_t ticket, bd_detection* out, int32_t* found,
+                              double* latency_ms);
+BD_API int32_t bd_server_get_stats(bd_server* server, bd_server_stats* out);
+
+/*
  * Tile statistics of one frame, for callers that cannot allocate memory.
  * No counterpart in the reference.
  *
@@ -152,6 +198,7 @@ BD_API int32_t bd_tile_stats_device_noalloc(const uint8_t* gray_device, int32_t 
 
 #ifdef __cplusplus
 static_assert(sizeof(bd_camera) == 16, "bd_camera layout changed");
+static_assert(sizeof(bd_server_stats) == 56, "bd_server_stats layout changed");
 #endif
 
 #endif /* BDCUDATAG_BDCUDATAG_GB300_H */
