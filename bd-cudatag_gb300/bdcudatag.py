@@ -21,6 +21,9 @@ FAMILY_TAG16H5 = 1
 OK = 0
 ERROR_INVALID_ARGUMENT = -1
 ERROR_CUDA = -2
+ERROR_OUT_OF_MEMORY = -3
+ERROR_NOT_SUPPORTED = -4
+ERROR_UNKNOWN = -5
 
 
 class Config(ctypes.Structure):

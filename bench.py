@@ -224,6 +224,118 @@ def measure_roofline(plan, frame_sets, peaks):
     }
 
 
+SERVE_SIZES = [(640, 480), (1280, 720), (1280, 800), (1600, 1304), (1920, 1080), (2560, 1440),
+               (3840, 2160)]
+
+
+def serving_trace(seconds: float, seed: int = 6324 + 5000):
+    """6 cameras: size drawn from 640x480..3840x2160, rate U(60, 120) fps,
+    Poisson arrivals; returns (cameras, arrivals [(t, camera, k)])."""
+    rng = np.random.default_rng(seed)
+    cams, arrivals = [], []
+    for c in range(6):
+        w, h = SERVE_SIZES[int(rng.integers(0, len(SERVE_SIZES)))]
+        fps = float(rng.uniform(60.0, 120.0))
+        cams.append((w, h, FAMILIES, fps))
+        t, k = float(rng.exponential(1.0 / fps)), 0
+        while t < seconds:
+            arrivals.append((t, c, k))
+            t += float(rng.exponential(1.0 / fps))
+            k += 1
+    arrivals.sort()
+    return cams, arrivals
+
+
+def measure_serving(seconds: float, pool_per_cam: int = 12):
+    """Config 5: continuous batching through bd_server versus a FIFO plain
+    per-frame detector fed by the same arrivals."""
+    import torch
+
+    import bdcudatag
+    import scenes
+
+    cams, arrivals = serving_trace(seconds)
+    pools = []
+    for c, (w, h, _, _) in enumerate(cams):
+        imgs, _ = scenes.render_many(5, [(w, h)] * pool_per_cam, threads=os.cpu_count() or 8,
+                                     base=scenes.base_seed(5) + 1000 * c)
+        pinned = torch.empty((pool_per_cam, h, w), dtype=torch.uint8, pin_memory=True)
+        pinned.numpy()[:] = np.stack(imgs)
+        pools.append((imgs, pinned))
+    server = bdcudatag.Server([(w, h, f) for w, h, f, _ in cams], device_budget=24 << 30,
+                              max_batches=4, queue_depth=16)
+    # warm-up: one frame per camera
+    for c in range(len(cams)):
+        server.wait(server.submit(c, pools[c][1][0]))
+    tickets: list = []
+    lat: list[float] = []
+    dropped = [0]
+    done = threading.Event()
+
+    def collector():
+        i = 0
+        while True:
+            while i >= len(tickets):
+                if done.is_set() and i >= len(tickets):
+                    return
+                time.sleep(0.0002)
+            rc, found, out, ms = server.wait(tickets[i])
+            lat.append(ms)
+            i += 1
+
+    th = threading.Thread(target=collector)
+    th.start()
+    t0 = time.perf_counter()
+    for t, c, k in arrivals:
+        while time.perf_counter() - t0 < t:
+            pass
+        tk = server.submit(c, pools[c][1][k % pool_per_cam])
+        if tk < 0:
+            dropped[0] += 1
+        else:
+            tickets.append(tk)
+    done.set()
+    th.join()
+    wall = time.perf_counter() - t0
+    st = server.stats()
+    server.close()
+    serve = {"frames_per_s": round(len(lat) / wall, 2), "p50_ms": round(pct(lat, 50), 4),
+             "p99_ms": round(pct(lat, 99), 4), "completed": len(lat), "dropped": dropped[0],
+             "offered_fps": round(len(arrivals) / seconds, 2), "seconds": seconds,
+             "batches": int(st.batches), "mean_batch_frames": round(st.mean_batch_frames, 3),
+             "plans": int(st.plans), "peak_inflight": int(st.peak_inflight),
+             "device_bytes": int(st.device_bytes)}
+    # Plain per-frame detect on the same arrivals: measured service time per
+    # (camera, frame) -- both families -- fed through a FIFO queue.
+    dets = [[bdcudatag.Detector(f, w, h) for f in (0, 1)] for w, h, _, _ in cams]
+    service = {}
+    for c in range(len(cams)):
+        for k in range(pool_per_cam):
+            img = pools[c][0][k]
+            for d in dets[c]:
+                d.detect(img)
+            ts = []
+            for _ in range(3):
+                t = time.perf_counter()
+                for d in dets[c]:
+                    d.detect(img)
+                ts.append(time.perf_counter() - t)
+            service[(c, k)] = float(np.median(ts))
+    free_at, plain_lat = 0.0, []
+    for t, c, k in arrivals:
+        start = max(t, free_at)
+        free_at = start + service[(c, k % pool_per_cam)]
+        plain_lat.append((free_at - t) * 1e3)
+    mean_service = float(np.mean([service[(c, k % pool_per_cam)] for _, c, k in arrivals]))
+    plain = {"p50_ms": round(pct(plain_lat, 50), 4), "p99_ms": round(pct(plain_lat, 99), 4),
+             "capacity_fps": round(1.0 / mean_service, 2),
+             "utilisation": round(len(arrivals) / seconds * mean_service, 3),
+             "method": "bd_detector_detect_host (one detector per camera and family), measured "
+                       "service time per frame, FIFO queue over the same arrival times"}
+    return {"cameras": [{"width": w, "height": h, "fps": round(f, 1)} for w, h, _, f in cams],
+            "server": serve, "plain": plain}
+
+
 def measure_cpu_baseline(frames, seconds_budget=12.0):
     import oracle
 
@@ -344,6 +456,7 @@ def bench_ours(args, rank, world, local_rank):
     roof = measure_roofline(plans[0], sets_dev, peaks)
     plain = measure_plain(frames, args.plain_frames)
     cpu = measure_cpu_baseline(frames)
+    serving = measure_serving(args.serving_seconds) if args.serving_seconds > 0 else None
     result_bytes = BATCH * ((32 + 2 * plans[0].max_detections * 84 + 255) // 256 * 256)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
@@ -364,6 +477,7 @@ def bench_ours(args, rank, world, local_rank):
         "e2e_speedup_vs_plain": round(e2e_value / plain["value"], 2),
         "roofline": roof,
         "cpu_baseline": cpu,
+        "serving": serving,
         "clocks": clocks.summary(),
         "gpu_launches": 9 * args.steps,
     }
@@ -378,6 +492,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--streams", type=int, default=4)
     ap.add_argument("--plain-frames", type=int, default=300)
+    ap.add_argument("--serving-seconds", type=float, default=60.0,
+                    help="length of the config-5 serving run (0: skip)")
     ap.add_argument("--quick", action="store_true",
                     help="profiling run: 64-frame pool, batched device-input loop only")
     args = ap.parse_args()
