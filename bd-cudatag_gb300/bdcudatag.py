@@ -73,6 +73,15 @@ class ServerStats(ctypes.Structure):
                 ("peak_inflight", ctypes.c_int32), ("device_bytes", ctypes.c_int64)]
 
 
+class RefineArgs(ctypes.Structure):
+    _fields_ = [("images", ctypes.c_void_p), ("image_pitch", ctypes.c_int64),
+                ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("stride", ctypes.c_int32),
+                ("count", ctypes.c_int32), ("image_index", ctypes.c_void_p),
+                ("corners", ctypes.c_void_p), ("templates", ctypes.c_void_p),
+                ("levels", ctypes.c_void_p), ("cells", ctypes.c_int32),
+                ("samples_per_cell", ctypes.c_int32)]
+
+
 class Camera(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32),
                 ("families", ctypes.c_uint32), ("reserved", ctypes.c_int32)]
@@ -100,6 +109,7 @@ GB300_SYMBOLS = [
     "bd_batch_query", "bd_tile_stats_device_noalloc",
     "bd_server_create", "bd_server_destroy", "bd_server_submit", "bd_server_wait",
     "bd_server_poll", "bd_server_get_stats",
+    "bd_tag_template", "bd_refine_forward", "bd_refine_backward", "bd_refine_gauss_newton",
 ]
 
 _LIB = None
@@ -172,6 +182,14 @@ def lib() -> ctypes.CDLL:
             getattr(L, n).argtypes = [_P, ctypes.c_int64, _P, _P, ctypes.POINTER(ctypes.c_double)]
             getattr(L, n).restype = ctypes.c_int32
         L.bd_server_get_stats.argtypes = [_P, ctypes.POINTER(ServerStats)]
+        L.bd_tag_template.argtypes = [ctypes.c_int32, ctypes.c_int32, _P]
+        L.bd_tag_template.restype = ctypes.c_int32
+        L.bd_refine_forward.argtypes = [ctypes.POINTER(RefineArgs), _P, _P, _P]
+        L.bd_refine_forward.restype = ctypes.c_int32
+        L.bd_refine_backward.argtypes = [ctypes.POINTER(RefineArgs), _P, _P, _P, _P]
+        L.bd_refine_backward.restype = ctypes.c_int32
+        L.bd_refine_gauss_newton.argtypes = [ctypes.POINTER(RefineArgs), _P, ctypes.c_int32, _P, _P]
+        L.bd_refine_gauss_newton.restype = ctypes.c_int32
         L.bd_batch_query.restype = ctypes.c_int32
         _LIB = L
     return _LIB
@@ -406,3 +424,26 @@ class Server:
 
     def __del__(self):
         self.close()
+
+
+def tag_template(family: int, tag_id: int) -> np.ndarray:
+    """(cells, cells) uint8 template of a tag, 1 = white (quiet zone included)."""
+    cells = 10 if family == 0 else 8
+    out = np.zeros(cells * cells, dtype=np.uint8)
+    n = lib().bd_tag_template(family, tag_id, out.ctypes.data)
+    if n < 0:
+        raise ValueError("bad family or id")
+    return out.reshape(cells, cells)
+
+
+def refine_args(images, corners, templates, image_index=None, levels=None,
+                samples_per_cell: int = 8) -> RefineArgs:
+    """Arguments over torch CUDA tensors: images [F, H, W] uint8, corners
+    [n, 8] float32, templates [n, cells, cells] uint8, image_index [n] int32,
+    levels [n, 2] float32."""
+    f, h, w = images.shape
+    return RefineArgs(images.data_ptr(), h * images.stride(1), w, h, images.stride(1),
+                      corners.shape[0], image_index.data_ptr() if image_index is not None else None,
+                      corners.data_ptr(), templates.data_ptr(),
+                      levels.data_ptr() if levels is not None else None, templates.shape[-1],
+                      samples_per_cell)

@@ -336,6 +336,97 @@ def measure_serving(seconds: float, pool_per_cam: int = 12):
             "server": serve, "plain": plain}
 
 
+def measure_refine(n_quads: int = 256, iterations: int = 5):
+    """Config 4: photometric Gauss-Newton on detected quads of 1280x800
+    frames, corners perturbed by U(-1.5, 1.5) px; corner error against ground
+    truth before and after, and the kernel times (CUDA events)."""
+    import itertools
+
+    import torch
+
+    import bdcudatag
+    import scenes
+
+    def matches(c, t):
+        c = np.asarray(c, np.float64).reshape(4, 2)
+        t = np.asarray(t, np.float64).reshape(4, 2)
+        side = np.mean([np.hypot(*(t[(j + 1) % 4] - t[j])) for j in range(4)])
+        return np.hypot(*(c.mean(0) - t.mean(0))) <= 0.75 * side
+
+    def err(c, t):
+        c = np.asarray(c, np.float64).reshape(4, 2)
+        t = np.asarray(t, np.float64).reshape(4, 2)
+        return min(np.mean([np.hypot(*(c[j] - t[p[j]])) for j in range(4)])
+                   for p in itertools.permutations(range(4)))
+
+    groups = {0: {"c": [], "t": [], "tm": [], "ix": []}, 1: {"c": [], "t": [], "tm": [], "ix": []}}
+    frames = []
+    dets = [bdcudatag.Detector(f, W, H) for f in (0, 1)]
+    fi = 0
+    while sum(len(g["c"]) for g in groups.values()) < n_quads and fi < 200:
+        img, tags = scenes.render_config(4, fi, W, H)
+        for fam in (0, 1):
+            n, d = dets[fam].detect(img)
+            for k in range(n):
+                for t in tags:
+                    if t.family == fam and t.id == d["id"][k] and matches(d["corners"][k], t.corners):
+                        g = groups[fam]
+                        g["c"].append(d["corners"][k].astype(np.float32))
+                        g["t"].append(t.corners.reshape(8))
+                        g["tm"].append(bdcudatag.tag_template(fam, int(t.id)))
+                        g["ix"].append(len(frames))
+        frames.append(img)
+        fi += 1
+    rng = np.random.default_rng(6324 + 4000)
+    images = torch.from_numpy(np.stack(frames)).cuda()
+    before, after, gn_ms, fb_ms, count = [], [], 0.0, 0.0, 0
+    for fam, g in groups.items():
+        if not g["c"]:
+            continue
+        c0 = np.stack(g["c"])
+        start = c0 + rng.uniform(-1.5, 1.5, c0.shape).astype(np.float32)
+        co = torch.from_numpy(start.copy()).cuda()
+        te = torch.from_numpy(np.stack(g["tm"])).cuda()
+        ix = torch.from_numpy(np.array(g["ix"], np.int32)).cuda()
+        args = bdcudatag.refine_args(images, co, te, ix, None, samples_per_cell=8)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        rc = bdcudatag.lib().bd_refine_gauss_newton(args, co.data_ptr(), iterations, None,
+                                                     torch.cuda.current_stream().cuda_stream)
+        e1.record()
+        torch.cuda.synchronize()
+        assert rc == 0, bdcudatag.last_error()
+        gn_ms += e0.elapsed_time(e1)
+        # forward + adjoint once, at the refined corners
+        n = co.shape[0]
+        cells = te.shape[-1]
+        res = torch.empty((n, cells * cells * 64), device="cuda")
+        gc = torch.empty_like(co)
+        gi = torch.zeros(images.shape, device="cuda", dtype=torch.float32)
+        args = bdcudatag.refine_args(images, co, te, ix, None, samples_per_cell=8)
+        s = torch.cuda.current_stream().cuda_stream
+        e0.record()
+        bdcudatag.lib().bd_refine_forward(args, res.data_ptr(), None, s)
+        bdcudatag.lib().bd_refine_backward(args, res.data_ptr(), gc.data_ptr(), gi.data_ptr(), s)
+        e1.record()
+        torch.cuda.synchronize()
+        fb_ms += e0.elapsed_time(e1)
+        refined = co.cpu().numpy()
+        before += [err(a, t) for a, t in zip(start, g["t"])]
+        after += [err(a, t) for a, t in zip(refined, g["t"])]
+        count += n
+    samples = sum(len(g["c"]) * (10 if f == 0 else 8) ** 2 * 64 for f, g in groups.items())
+    return {"quads": count, "frames": len(frames), "iterations": iterations,
+            "corner_err_before_px": {"mean": round(float(np.mean(before)), 4),
+                                     "median": round(float(np.median(before)), 4)},
+            "corner_err_after_px": {"mean": round(float(np.mean(after)), 4),
+                                    "median": round(float(np.median(after)), 4),
+                                    "p95": round(float(np.percentile(after, 95)), 4)},
+            "gauss_newton_ms": round(gn_ms, 4), "forward_backward_ms": round(fb_ms, 4),
+            "samples_per_pass": samples}
+
+
 def measure_cpu_baseline(frames, seconds_budget=12.0):
     import oracle
 
@@ -457,6 +548,7 @@ def bench_ours(args, rank, world, local_rank):
     plain = measure_plain(frames, args.plain_frames)
     cpu = measure_cpu_baseline(frames)
     serving = measure_serving(args.serving_seconds) if args.serving_seconds > 0 else None
+    refine = measure_refine()
     result_bytes = BATCH * ((32 + 2 * plans[0].max_detections * 84 + 255) // 256 * 256)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
@@ -478,6 +570,7 @@ def bench_ours(args, rank, world, local_rank):
         "roofline": roof,
         "cpu_baseline": cpu,
         "serving": serving,
+        "refine": refine,
         "clocks": clocks.summary(),
         "gpu_launches": 9 * args.steps,
     }

@@ -159,6 +159,54 @@ BD_API int32_t bd_server_poll(bd_server* server, int64_t ticket, bd_detection* o
 BD_API int32_t bd_server_get_stats(bd_server* server, bd_server_stats* out);
 
 /*
+ * Photometric corner refinement.  No counterpart in the reference; the
+ * reference's edge-line fit stays the default inside detection.
+ *
+ * For quad q with corners c (TL TR BR BL, pixel-index coordinates, as in
+ * bd_detection), H(c) is the square-to-quad homography of the decoder and
+ * the template is the tag's cell grid plus a one-cell quiet zone (`cells`
+ * per side: 10 for tag36h11, 8 for tag16h5; bd_tag_template builds it),
+ * sampled at samples_per_cell^2 points per cell.  Residual of sample s:
+ *     r_s = I(H(c) * (u_s, v_s)) - (black + (white - black) * template_s)
+ * with I the frame sampled bilinearly; samples that leave the frame are 0.
+ * Loss per quad = 0.5 * sum_s r_s^2.  All pointers are device memory;
+ * calls are asynchronous on cuda_stream.
+ */
+typedef struct bd_refine_args {
+    const uint8_t* images;       /* frames, image_pitch bytes apart */
+    int64_t image_pitch;
+    int32_t width;
+    int32_t height;
+    int32_t stride;              /* row stride in bytes (>= width) */
+    int32_t count;               /* number of quads */
+    const int32_t* image_index;  /* frame of each quad, or NULL: frame 0 */
+    const float* corners;        /* count * 8 */
+    const uint8_t* templates;    /* count * cells * cells, 1 = white */
+    const float* levels;         /* count * 2 (black, white), or NULL: 0 and 255 */
+    int32_t cells;
+    int32_t samples_per_cell;
+} bd_refine_args;
+
+/* Writes the (bits + 4)^2 cell template of tag `id` (1 = white: quiet zone
+ * ring, black border ring, data cells row-major) and returns bits + 4, or a
+ * negative bd_status. */
+BD_API int32_t bd_tag_template(int32_t family, int32_t id, uint8_t* cells_out);
+/* residuals: count * cells^2 * samples_per_cell^2 (or NULL); loss: count. */
+BD_API int32_t bd_refine_forward(const bd_refine_args* args, float* residuals, float* loss,
+                                 void* cuda_stream);
+/* Adjoint: given dL/dr for every residual, writes dL/dcorners (count * 8)
+ * and, when grad_images is not NULL, ADDS dL/dI into it (float frames laid
+ * out like `images`, pitch image_pitch elements, row stride `stride`). */
+BD_API int32_t bd_refine_backward(const bd_refine_args* args, const float* grad_residuals,
+                                  float* grad_corners, float* grad_images, void* cuda_stream);
+/* Gauss-Newton on the corners, `iterations` damped steps in one launch;
+ * with levels NULL the black / white levels are re-estimated from the
+ * template cells every step.  loss (count, or NULL) receives the final
+ * loss. */
+BD_API int32_t bd_refine_gauss_newton(const bd_refine_args* args, float* corners_inout,
+                                      int32_t iterations, float* loss, void* cuda_stream);
+
+/*
  * Tile statistics of one frame, for callers that cannot allocate memory.
  * No counterpart in the reference.
  *
@@ -199,6 +247,7 @@ BD_API int32_t bd_tile_stats_device_noalloc(const uint8_t* gray_device, int32_t 
 #ifdef __cplusplus
 static_assert(sizeof(bd_camera) == 16, "bd_camera layout changed");
 static_assert(sizeof(bd_server_stats) == 56, "bd_server_stats layout changed");
+static_assert(sizeof(bd_refine_args) == 72, "bd_refine_args layout changed");
 #endif
 
 #endif /* BDCUDATAG_BDCUDATAG_GB300_H */
