@@ -142,7 +142,10 @@ def test_forward_matches_fp64(quads):
     r64, l64 = ref_forward(im.double(), co.double(), te, ix, lv.double())
     torch.cuda.synchronize()
     assert torch.allclose(loss.double(), l64, rtol=1e-4, atol=1e-3)
-    assert (res.double() - r64).abs().max().item() < 2e-2
+    # FP32 sample positions carry ~1e-4 px of rounding near x ~ 1000; on an
+    # edge of 255 DN/px that is ~0.03 DN of residual.
+    diff = (res.double() - r64).abs()
+    assert diff.max().item() < 0.1 and diff.mean().item() < 2e-3
 
 
 def test_adjoint_matches_fp64_autograd_and_finite_differences(quads):
