@@ -82,6 +82,11 @@ class RefineArgs(ctypes.Structure):
                 ("samples_per_cell", ctypes.c_int32)]
 
 
+class LaunchConfig(ctypes.Structure):
+    _fields_ = [("stats_rows", ctypes.c_int32), ("fit_warps", ctypes.c_int32),
+                ("fit_ctas_per_sm", ctypes.c_int32), ("decode_ctas_per_sm", ctypes.c_int32)]
+
+
 class Camera(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32),
                 ("families", ctypes.c_uint32), ("reserved", ctypes.c_int32)]
@@ -110,6 +115,7 @@ GB300_SYMBOLS = [
     "bd_server_create", "bd_server_destroy", "bd_server_submit", "bd_server_wait",
     "bd_server_poll", "bd_server_get_stats",
     "bd_tag_template", "bd_refine_forward", "bd_refine_backward", "bd_refine_gauss_newton",
+    "bd_batch_get_launch", "bd_batch_set_launch", "bd_batch_autotune",
 ]
 
 _LIB = None
@@ -182,6 +188,12 @@ def lib() -> ctypes.CDLL:
             getattr(L, n).argtypes = [_P, ctypes.c_int64, _P, _P, ctypes.POINTER(ctypes.c_double)]
             getattr(L, n).restype = ctypes.c_int32
         L.bd_server_get_stats.argtypes = [_P, ctypes.POINTER(ServerStats)]
+        L.bd_batch_get_launch.argtypes = [_P, ctypes.POINTER(LaunchConfig)]
+        L.bd_batch_set_launch.argtypes = [_P, ctypes.POINTER(LaunchConfig)]
+        L.bd_batch_set_launch.restype = ctypes.c_int32
+        L.bd_batch_autotune.argtypes = [_P, _P, _P, ctypes.c_int32, ctypes.POINTER(LaunchConfig),
+                                        ctypes.POINTER(ctypes.c_float)]
+        L.bd_batch_autotune.restype = ctypes.c_int32
         L.bd_tag_template.argtypes = [ctypes.c_int32, ctypes.c_int32, _P]
         L.bd_tag_template.restype = ctypes.c_int32
         L.bd_refine_forward.argtypes = [ctypes.POINTER(RefineArgs), _P, _P, _P]
@@ -351,6 +363,31 @@ class Batch:
         if r < 0:
             raise RuntimeError(f"batch query failed ({r}): {last_error()}")
         return r == 1
+
+    def launch(self) -> dict:
+        lc = LaunchConfig()
+        lib().bd_batch_get_launch(self.handle, ctypes.byref(lc))
+        return {f: getattr(lc, f) for f, _ in LaunchConfig._fields_}
+
+    def set_launch(self, **fields) -> None:
+        lc = LaunchConfig()
+        lib().bd_batch_get_launch(self.handle, ctypes.byref(lc))
+        for k, v in fields.items():
+            setattr(lc, k, v)
+        rc = lib().bd_batch_set_launch(self.handle, ctypes.byref(lc))
+        if rc != 0:
+            raise RuntimeError(f"set_launch failed ({rc}): {last_error()}")
+
+    def autotune(self, frames_device, strides=None, iterations: int = 20):
+        self._set(frames_device, strides)
+        lc = LaunchConfig()
+        ms = ctypes.c_float(0.0)
+        rc = lib().bd_batch_autotune(self.handle, ctypes.cast(self._ptrs, _P),
+                                     self._strides.ctypes.data, iterations, ctypes.byref(lc),
+                                     ctypes.byref(ms))
+        if rc != 0:
+            raise RuntimeError(f"autotune failed ({rc}): {last_error()}")
+        return {f: getattr(lc, f) for f, _ in LaunchConfig._fields_}, ms.value
 
     def host_frame(self, i: int) -> np.ndarray:
         w, h, _ = self.cameras[i]

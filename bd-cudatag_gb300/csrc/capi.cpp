@@ -449,6 +449,54 @@ int32_t bd_batch_set_stream(bd_batch* batch, void* cuda_stream) {
     return BD_OK;
 }
 
+int32_t bd_batch_get_launch(const bd_batch* batch, bd_launch_config* out) {
+    if (!batch || !out) return BD_ERROR_INVALID_ARGUMENT;
+    const bdgb::LaunchConfig& lc = batch->plan->launch();
+    out->stats_rows = lc.stats_rows;
+    out->fit_warps = lc.fit_warps;
+    out->fit_ctas_per_sm = lc.fit_ctas_per_sm;
+    out->decode_ctas_per_sm = lc.decode_ctas_per_sm;
+    return BD_OK;
+}
+
+int32_t bd_batch_set_launch(bd_batch* batch, const bd_launch_config* launch) {
+    if (!batch || !launch) {
+        set_error("null batch or launch config");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    bdgb::LaunchConfig lc;
+    lc.stats_rows = launch->stats_rows;
+    lc.fit_warps = launch->fit_warps;
+    lc.fit_ctas_per_sm = launch->fit_ctas_per_sm;
+    lc.decode_ctas_per_sm = launch->decode_ctas_per_sm;
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    std::string error;
+    if (batch->plan->set_launch(lc, &error) != 0) {
+        set_error(error);
+        return error.rfind("launch config", 0) == 0 ? BD_ERROR_INVALID_ARGUMENT : BD_ERROR_CUDA;
+    }
+    return BD_OK;
+}
+
+int32_t bd_batch_autotune(bd_batch* batch, const uint8_t* const* frames_device,
+                          const int32_t* strides, int32_t iterations, bd_launch_config* best_out,
+                          float* best_ms_out) {
+    const int bad = batch_check(batch, frames_device, strides);
+    if (bad != BD_OK) return bad;
+    std::string error;
+    float ms = 0.0f;
+    {
+        const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+        if (batch->plan->autotune(frames_device, strides, iterations, &ms, &error) != 0) {
+            set_error(error);
+            return BD_ERROR_CUDA;
+        }
+    }
+    if (best_out) bd_batch_get_launch(batch, best_out);
+    if (best_ms_out) *best_ms_out = ms;
+    return BD_OK;
+}
+
 int32_t bd_stage_count(void) { return bdgb::kStageCount; }
 
 const char* bd_stage_name(int32_t stage) {

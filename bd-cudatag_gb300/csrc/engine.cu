@@ -85,6 +85,8 @@ struct Plan::Impl {
     cudaGraphExec_t graph_fixed = nullptr;   // pipeline + D2H on the plan's device frames
     cudaGraphExec_t graph_device = nullptr;  // caller device frames
     cudaStream_t user_stream = nullptr;      // caller stream for submits (null: own stream)
+    LaunchConfig launch_cfg;
+    int sm_count = 152;
     cudaEvent_t stage_events[kStageCount + 1] = {};
     bool pending = false;
 
@@ -93,9 +95,7 @@ struct Plan::Impl {
     ~Impl() {
         if (stream) cudaStreamSynchronize(stream);
         if (user_stream) cudaStreamSynchronize(user_stream);
-        if (graph_host) cudaGraphExecDestroy(graph_host);
-        if (graph_fixed) cudaGraphExecDestroy(graph_fixed);
-        if (graph_device) cudaGraphExecDestroy(graph_device);
+        destroy_graphs();
         for (cudaEvent_t e : stage_events) {
             if (e) cudaEventDestroy(e);
         }
@@ -118,7 +118,8 @@ struct Plan::Impl {
                             cudaMemcpyHostToDevice, s);
         }
         cudaMemsetAsync(states, 0, states_bytes, s);
-        enqueue_pipeline(dev_desc, host_desc, mode == 2 ? io_caller : io_fixed, s, events);
+        enqueue_pipeline(dev_desc, host_desc, mode == 2 ? io_caller : io_fixed, s, launch_cfg, sm_count,
+                         events);
         cudaMemcpyAsync(results_pinned, results_dev, results_bytes, cudaMemcpyDeviceToHost, s);
     }
 
@@ -129,6 +130,20 @@ struct Plan::Impl {
         } else {
             enqueue(mode, s);
         }
+    }
+
+    void destroy_graphs() {
+        if (graph_host) cudaGraphExecDestroy(graph_host);
+        if (graph_fixed) cudaGraphExecDestroy(graph_fixed);
+        if (graph_device) cudaGraphExecDestroy(graph_device);
+        graph_host = graph_fixed = graph_device = nullptr;
+    }
+
+    void capture_all() {
+        destroy_graphs();
+        if (!capture(0, &graph_host)) graph_host = nullptr;
+        if (!capture(1, &graph_fixed)) graph_fixed = nullptr;
+        if (!capture(2, &graph_device)) graph_device = nullptr;
     }
 
     bool capture(int mode, cudaGraphExec_t* out) {
@@ -186,6 +201,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
         cudaGetLastError();
         return fail("cudaFuncSetAttribute failed");
     }
+    cudaDeviceGetAttribute(&im.sm_count, cudaDevAttrMultiProcessorCount, im.device);
 
     const int nf = static_cast<int>(frames.size());
     const int md = config.max_detections;
@@ -268,6 +284,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     }
     hd.band_prefix[nf] = bands;
     hd.total_bands = bands;
+    set_stats_rows(hd, im.launch_cfg.stats_rows);
     plan->arena_bytes_ = carve.off;
 
     st = cudaMalloc(&im.arena, carve.off);
@@ -338,9 +355,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     if (config.use_graph) {
         // A failed capture falls back to direct launches (reference
         // gpu_detector.cu:2051-2056).
-        if (!im.capture(0, &im.graph_host)) im.graph_host = nullptr;
-        if (!im.capture(1, &im.graph_fixed)) im.graph_fixed = nullptr;
-        if (!im.capture(2, &im.graph_device)) im.graph_device = nullptr;
+        im.capture_all();
     }
     return plan;
 }
@@ -481,6 +496,79 @@ int Plan::submit_slots(const uint8_t* const* frames, const int32_t* strides, std
         return -1;
     }
     im.pending = true;
+    return 0;
+}
+
+const LaunchConfig& Plan::launch() const { return impl_->launch_cfg; }
+
+int Plan::set_launch(const LaunchConfig& lc, std::string* error) {
+    Impl& im = *impl_;
+    if (!(lc.stats_rows == 1 || lc.stats_rows == 2 || lc.stats_rows == 4) ||
+        !(lc.fit_warps == 4 || lc.fit_warps == 8) || lc.fit_ctas_per_sm < 1 ||
+        lc.fit_ctas_per_sm > 32 || lc.decode_ctas_per_sm < 1 || lc.decode_ctas_per_sm > 32) {
+        if (error) *error = "launch config out of range";
+        return -1;
+    }
+    if (im.pending && wait(error) != 0) return -1;
+    cudaStreamSynchronize(im.stream);
+    im.launch_cfg = lc;
+    set_stats_rows(im.host_desc, lc.stats_rows);
+    const cudaError_t st = cudaMemcpy(im.dev_desc, &im.host_desc, sizeof(BatchDesc),
+                                      cudaMemcpyHostToDevice);
+    if (st != cudaSuccess) {
+        if (error) *error = cuda_error("cudaMemcpy(plan)", st);
+        return -1;
+    }
+    if (config_.use_graph) im.capture_all();
+    return 0;
+}
+
+int Plan::autotune(const uint8_t* const* frames, const int32_t* strides, int iterations,
+                   float* best_ms, std::string* error) {
+    Impl& im = *impl_;
+    iterations = std::max(iterations, 3);
+    std::vector<float> times(iterations);
+    auto measure = [&](const LaunchConfig& lc, float* ms) -> int {
+        if (set_launch(lc, error) != 0) return -1;
+        for (int k = 0; k < 3; ++k) {
+            if (run_device(frames, strides, error) != 0) return -1;
+        }
+        for (int k = 0; k < iterations; ++k) {
+            if (run_device(frames, strides, error) != 0) return -1;
+            times[k] = last_gpu_ms_;
+        }
+        std::vector<float> sorted = times;
+        std::sort(sorted.begin(), sorted.end());
+        *ms = sorted[sorted.size() / 2];
+        return 0;
+    };
+    LaunchConfig best = im.launch_cfg;
+    float best_t = 0.0f;
+    if (measure(best, &best_t) != 0) return -1;
+    const int stats_rows[] = {1, 2, 4};
+    const int fit_warps[] = {8, 4};
+    const int fit_ctas[] = {2, 4, 8, 16};
+    const int dec_ctas[] = {2, 4, 6, 8};
+    auto try_values = [&](auto field, const int* values, int n) -> int {
+        for (int i = 0; i < n; ++i) {
+            LaunchConfig lc = best;
+            lc.*field = values[i];
+            if (lc.*field == best.*field) continue;
+            float t = 0.0f;
+            if (measure(lc, &t) != 0) return -1;
+            if (t < best_t) {
+                best_t = t;
+                best = lc;
+            }
+        }
+        return 0;
+    };
+    if (try_values(&LaunchConfig::stats_rows, stats_rows, 3) != 0) return -1;
+    if (try_values(&LaunchConfig::fit_warps, fit_warps, 2) != 0) return -1;
+    if (try_values(&LaunchConfig::fit_ctas_per_sm, fit_ctas, 4) != 0) return -1;
+    if (try_values(&LaunchConfig::decode_ctas_per_sm, dec_ctas, 4) != 0) return -1;
+    if (set_launch(best, error) != 0) return -1;
+    if (best_ms) *best_ms = best_t;
     return 0;
 }
 

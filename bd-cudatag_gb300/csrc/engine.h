@@ -13,6 +13,7 @@
 namespace bdgb {
 
 struct FrameResultHeader;
+struct LaunchConfig;
 
 struct PlanFrame {
     int width = 0;
@@ -64,6 +65,14 @@ public:
     // Host frames (page-locked or not) are copied to the plan's device
     // buffers; results as for submit_host.
     int submit_slots(const uint8_t* const* frames, const int32_t* strides, std::string* error);
+
+    // Launch shapes (results do not depend on them).  set_launch re-captures
+    // the graphs; autotune times candidate shapes on `iterations` device-input
+    // runs of `frames` (coordinate descent) and keeps the fastest.
+    int set_launch(const LaunchConfig& launch, std::string* error);
+    const LaunchConfig& launch() const;
+    int autotune(const uint8_t* const* frames, const int32_t* strides, int iterations,
+                 float* best_ms, std::string* error);
 
     // Stream for later submits (a cudaStream_t; null: the plan's own).
     void set_stream(void* stream);

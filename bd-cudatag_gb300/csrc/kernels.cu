@@ -30,6 +30,7 @@
 
 #include <cfloat>
 #include <climits>
+#include <algorithm>
 #include <cstdint>
 
 #include "detmath.h"
@@ -117,87 +118,102 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
     __shared__ int s_best_idx[2];
 
     const int tid = threadIdx.x;
-    const int fi = frame_of_band(b, blockIdx.x);
+    // CTA c of a frame covers tile rows [c * R, c * R + R), R = stats_rows.
+    int fi = 0;
+    {
+        int lo = 0, hi = b->frames - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (b->stats_prefix[mid] <= static_cast<int>(blockIdx.x)) lo = mid; else hi = mid - 1;
+        }
+        fi = lo;
+    }
     if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
-    const int ty = blockIdx.x - b->band_prefix[fi];
+    const int R = b->stats_rows;
+    const int cta = blockIdx.x - b->stats_prefix[fi];
+    const int n_ctas = b->stats_prefix[fi + 1] - b->stats_prefix[fi];
     FrameState* st = d.state;
 
     s_span[tid] = 0;
     if (tid < 64) s_mean[tid] = 0;
-    if (tid == 0) {
-        s_lo = INT_MAX;
-        s_hi = -1;
-    }
-    __syncthreads();
 
     const uint8_t* gray = io[fi].gray;
     const int64_t stride = io[fi].stride;
     const int W = d.width, H = d.height, tw = d.tile_w;
-    const int y0 = ty * kTile;
-    const int rows = min(kTile, H - y0);
     const bool vec = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 7u) == 0;
-    int lo = INT_MAX, hi = -1;
-    for (int tx = tid; tx < tw; tx += blockDim.x) {
-        const int x0 = tx * kTile;
-        const int cols = min(kTile, W - x0);
-        const uint8_t* p = gray + static_cast<int64_t>(y0) * stride + x0;
-        uint32_t mn, mx, sum = 0;
-        if (vec && cols == kTile) {
-            uint32_t vmin = 0xffffffffu, vmax = 0u;
-            for (int r = 0; r < rows; ++r) {
-                const uint2 v = *reinterpret_cast<const uint2*>(p + r * stride);
-                vmin = __vminu4(vmin, __vminu4(v.x, v.y));
-                vmax = __vmaxu4(vmax, __vmaxu4(v.x, v.y));
-                sum = __dp4a(v.x, 0x01010101u, sum);
-                sum = __dp4a(v.y, 0x01010101u, sum);
-            }
-            mn = min(min(vmin & 0xffu, (vmin >> 8) & 0xffu), min((vmin >> 16) & 0xffu, vmin >> 24));
-            mx = max(max(vmax & 0xffu, (vmax >> 8) & 0xffu), max((vmax >> 16) & 0xffu, vmax >> 24));
-        } else {
-            mn = 255u;
-            mx = 0u;
-            for (int r = 0; r < rows; ++r) {
-                for (int c = 0; c < cols; ++c) {
-                    const uint32_t v = p[r * stride + c];
-                    mn = min(mn, v);
-                    mx = max(mx, v);
-                    sum += v;
+    const int ty_end = min((cta + 1) * R, d.tile_h);
+    for (int ty = cta * R; ty < ty_end; ++ty) {
+        if (tid == 0) {
+            s_lo = INT_MAX;
+            s_hi = -1;
+        }
+        __syncthreads();
+        const int y0 = ty * kTile;
+        const int rows = min(kTile, H - y0);
+        int lo = INT_MAX, hi = -1;
+        for (int tx = tid; tx < tw; tx += blockDim.x) {
+            const int x0 = tx * kTile;
+            const int cols = min(kTile, W - x0);
+            const uint8_t* p = gray + static_cast<int64_t>(y0) * stride + x0;
+            uint32_t mn, mx, sum = 0;
+            if (vec && cols == kTile) {
+                uint32_t vmin = 0xffffffffu, vmax = 0u;
+                for (int r = 0; r < rows; ++r) {
+                    const uint2 v = *reinterpret_cast<const uint2*>(p + r * stride);
+                    vmin = __vminu4(vmin, __vminu4(v.x, v.y));
+                    vmax = __vmaxu4(vmax, __vmaxu4(v.x, v.y));
+                    sum = __dp4a(v.x, 0x01010101u, sum);
+                    sum = __dp4a(v.y, 0x01010101u, sum);
+                }
+                mn = min(min(vmin & 0xffu, (vmin >> 8) & 0xffu), min((vmin >> 16) & 0xffu, vmin >> 24));
+                mx = max(max(vmax & 0xffu, (vmax >> 8) & 0xffu), max((vmax >> 16) & 0xffu, vmax >> 24));
+            } else {
+                mn = 255u;
+                mx = 0u;
+                for (int r = 0; r < rows; ++r) {
+                    for (int c = 0; c < cols; ++c) {
+                        const uint32_t v = p[r * stride + c];
+                        mn = min(mn, v);
+                        mx = max(mx, v);
+                        sum += v;
+                    }
                 }
             }
+            const uint32_t count = static_cast<uint32_t>(rows * cols);
+            const uint32_t mean = (sum + count / 2) / count;
+            const int idx = ty * tw + tx;
+            d.tile_min[idx] = static_cast<uint8_t>(mn);
+            d.tile_max[idx] = static_cast<uint8_t>(mx);
+            atomicAdd(&s_span[(mx - mn) & 0xffu], 1u);
+            atomicAdd(&s_mean[mean >> 2], 1u);
+            if (static_cast<int>(mx - mn) >= kMinTileContrast) {
+                lo = min(lo, tx);
+                hi = max(hi, tx);
+            }
         }
-        const uint32_t count = static_cast<uint32_t>(rows * cols);
-        const uint32_t mean = (sum + count / 2) / count;
-        const int idx = ty * tw + tx;
-        d.tile_min[idx] = static_cast<uint8_t>(mn);
-        d.tile_max[idx] = static_cast<uint8_t>(mx);
-        atomicAdd(&s_span[(mx - mn) & 0xffu], 1u);
-        atomicAdd(&s_mean[mean >> 2], 1u);
-        if (static_cast<int>(mx - mn) >= kMinTileContrast) {
-            lo = min(lo, tx);
-            hi = max(hi, tx);
+        lo = __reduce_min_sync(kFull, lo);
+        hi = __reduce_max_sync(kFull, hi);
+        if ((tid & 31) == 0 && hi >= 0) {
+            atomicMin(&s_lo, lo);
+            atomicMax(&s_hi, hi);
         }
-    }
-    lo = __reduce_min_sync(kFull, lo);
-    hi = __reduce_max_sync(kFull, hi);
-    if ((tid & 31) == 0 && hi >= 0) {
-        atomicMin(&s_lo, lo);
-        atomicMax(&s_hi, hi);
-    }
-    __syncthreads();
-    if (tid == 0) {
-        d.row_lo[ty] = s_hi >= 0 ? s_lo : -1;
-        d.row_hi[ty] = s_hi;
-        if (s_hi >= 0) {
-            atomicMax(&st->top_enc, static_cast<uint32_t>(d.tile_h - ty));
-            atomicMax(&st->bottom_enc, static_cast<uint32_t>(ty + 1));
+        __syncthreads();
+        if (tid == 0) {
+            d.row_lo[ty] = s_hi >= 0 ? s_lo : -1;
+            d.row_hi[ty] = s_hi;
+            if (s_hi >= 0) {
+                atomicMax(&st->top_enc, static_cast<uint32_t>(d.tile_h - ty));
+                atomicMax(&st->bottom_enc, static_cast<uint32_t>(ty + 1));
+            }
         }
+        __syncthreads();
     }
     if (s_span[tid]) atomicAdd(&st->span_hist[tid], s_span[tid]);
     if (tid < 64 && s_mean[tid]) atomicAdd(&st->mean_hist[tid], s_mean[tid]);
     __threadfence();
     __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&st->done_stats, 1u) == static_cast<uint32_t>(d.tile_h - 1);
+    if (tid == 0) s_last = atomicAdd(&st->done_stats, 1u) == static_cast<uint32_t>(n_ctas - 1);
     __syncthreads();
     if (!s_last) return;
     __threadfence();
@@ -1191,14 +1207,13 @@ __device__ float apply_refined_lines(float quad[4][2], const float lines[4][4], 
     return moved;
 }
 
-constexpr int kFitThreads = 256;
-constexpr int kFitWarps = kFitThreads / 32;
-
 // Flattened (frame, candidate) work list: CTA c takes items c, c + grid, ...
-// The hull is built once per candidate; warps 0-3 refine the quad for the
-// frame's first requested family and warps 4-7 for the second, concurrently.
-__global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict__ b,
-                                                     const FrameIO* __restrict__ io) {
+// The hull is built once per candidate; with 8 warps, warps 0-3 refine the
+// quad for the frame's first requested family and warps 4-7 for the second,
+// concurrently; with 4 warps the families are refined one after the other.
+template <int kFitWarps>
+__global__ void __launch_bounds__(kFitWarps * 32) k_fit(const BatchDesc* __restrict__ b,
+                                                        const FrameIO* __restrict__ io) {
     __shared__ uint32_t boundary[2 * kMaxBoundaryRows];
     __shared__ float probe_dot[kFitWarps][kFitDirections];
     __shared__ uint32_t probe_point[kFitWarps][kFitDirections];
@@ -1374,8 +1389,9 @@ __global__ void __launch_bounds__(kFitThreads) k_fit(const BatchDesc* __restrict
             __syncthreads();
             continue;
         }
-        if (d.refine_edges) {
-            const int slot = warp >> 2;
+        constexpr int kSlotsPerPass = kFitWarps / 4;
+        for (int pass0 = 0; d.refine_edges && pass0 < nfam; pass0 += kSlotsPerPass) {
+            const int slot = pass0 + (warp >> 2);
             const int edge = warp & 3;
             const bool mine = slot < nfam;
             const int dim = family_dim(fam_of_slot[slot < nfam ? slot : 0]);
@@ -1807,7 +1823,7 @@ const char* const kStageNames[kStageCount] = {
     "cand_emit", "fit", "decode", "finalize"};
 
 void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* io, void* stream_ptr,
-                      void* const* stage_events) {
+                      const LaunchConfig& lc, int sm_count, void* const* stage_events) {
     cudaStream_t s = static_cast<cudaStream_t>(stream_ptr);
     auto mark = [&](int k) {
         if (stage_events) cudaEventRecord(static_cast<cudaEvent_t>(stage_events[k]), s);
@@ -1819,10 +1835,10 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
         cand_total += hd.f[f].max_candidates;
         dec_total += hd.f[f].max_candidates * __builtin_popcount(hd.f[f].families & 3u);
     }
-    const int fit_grid = cand_total < 152 * 8 ? cand_total : 152 * 8;
-    const int dec_grid = dec_total < 152 * 6 ? dec_total : 152 * 6;
+    const int fit_grid = std::max(1, std::min(cand_total, sm_count * lc.fit_ctas_per_sm));
+    const int dec_grid = std::max(1, std::min(dec_total, sm_count * lc.decode_ctas_per_sm));
     mark(0);
-    k_stats<<<bands, 256, 0, s>>>(dd, io);
+    k_stats<<<hd.stats_ctas, 256, 0, s>>>(dd, io);
     mark(1);
     k_binarize_runs<<<bands, 256, kBandSmemBytes, s>>>(dd, io);
     mark(2);
@@ -1834,9 +1850,13 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     mark(5);
     k_cand_emit<<<bands, 256, 0, s>>>(dd, io);
     mark(6);
-    k_fit<<<fit_grid > 0 ? fit_grid : 1, kFitThreads, 0, s>>>(dd, io);
+    if (lc.fit_warps == 4) {
+        k_fit<4><<<fit_grid, 128, 0, s>>>(dd, io);
+    } else {
+        k_fit<8><<<fit_grid, 256, 0, s>>>(dd, io);
+    }
     mark(7);
-    k_decode<<<dec_grid > 0 ? dec_grid : 1, kDecodeThreads, 0, s>>>(dd, io);
+    k_decode<<<dec_grid, kDecodeThreads, 0, s>>>(dd, io);
     mark(8);
     k_finalize<<<hd.frames * 2, kFinalThreads, 0, s>>>(dd);
     mark(9);

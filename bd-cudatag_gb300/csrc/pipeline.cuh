@@ -103,8 +103,31 @@ struct BatchDesc {
     int32_t frames;
     int32_t total_bands;
     int32_t band_prefix[kMaxFrames + 1];  // exclusive prefix of tile_h over frames
+    int32_t stats_rows;                   // tile rows per k_stats CTA
+    int32_t stats_ctas;
+    int32_t stats_prefix[kMaxFrames + 1]; // exclusive prefix of ceil(tile_h / stats_rows)
     FrameDesc f[kMaxFrames];
 };
+
+// Launch shapes that do not change any result (tuned per plan).
+struct LaunchConfig {
+    int stats_rows = 1;        // tile rows per k_stats CTA: 1, 2 or 4
+    int fit_warps = 8;         // 8: both families refined concurrently; 4: one after the other
+    int fit_ctas_per_sm = 8;   // persistent fit grid = SMs * this (capped by the work)
+    int decode_ctas_per_sm = 6;
+};
+
+// Fills the stats fields of a host BatchDesc for `rows` tile rows per CTA.
+inline void set_stats_rows(BatchDesc& d, int rows) {
+    d.stats_rows = rows;
+    int run = 0;
+    for (int f = 0; f < d.frames; ++f) {
+        d.stats_prefix[f] = run;
+        run += (d.f[f].tile_h + rows - 1) / rows;
+    }
+    d.stats_prefix[d.frames] = run;
+    d.stats_ctas = run;
+}
 
 BDGB_HD inline bd_detection* result_detections(FrameResultHeader* h) {
     return reinterpret_cast<bd_detection*>(h + 1);
@@ -124,6 +147,7 @@ constexpr int kStageCount = 9;
 int prepare_pipeline();
 extern const char* const kStageNames[kStageCount];
 void enqueue_pipeline(const BatchDesc* device_desc, const BatchDesc& host_desc,
-                      const FrameIO* device_io, void* stream, void* const* stage_events = nullptr);
+                      const FrameIO* device_io, void* stream, const LaunchConfig& launch,
+                      int sm_count, void* const* stage_events = nullptr);
 
 }  // namespace bdgb

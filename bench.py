@@ -118,7 +118,7 @@ def pct(values, q):
     return float(np.percentile(np.asarray(values), q)) if len(values) else None
 
 
-def run_batched(plans, streams, frame_sets, steps, warmup, device: bool):
+def run_batched(plans, streams, frame_sets, steps, warmup, device: bool, strides=None):
     """Round-robin batches over the plans; returns (elapsed ms by CUDA
     events, per-batch latencies in ms)."""
     import torch
@@ -146,7 +146,7 @@ def run_batched(plans, streams, frame_sets, steps, warmup, device: bool):
                 drain(i, lat)
             frames = frame_sets[(offset + k) % len(frame_sets)]
             issued[i] = time.perf_counter()
-            plans[i].submit(frames, [W] * BATCH, device=device)
+            plans[i].submit(frames, strides or [W] * BATCH, device=device)
         for i in list(issued):
             while not plans[i].query():
                 pass
@@ -244,6 +244,52 @@ def serving_trace(seconds: float, seed: int = 6324 + 5000):
             k += 1
     arrivals.sort()
     return cams, arrivals
+
+
+CONFIG3_SIZES = [(640, 480), (1280, 800), (1600, 1304), (1920, 1080)] * 4
+
+
+def measure_config3(steps: int, streams: int = 4, pool_batches: int = 8):
+    """Config 3: 16-frame batches of uneven sizes (4 each of 640x480, 1280x800,
+    1600x1304, 1920x1080), both families, autotuned launch shapes; frames/s
+    with frames resident in HBM, and a bit-exact check of one batch against
+    single-frame detection."""
+    import torch
+
+    import bdcudatag
+    import scenes
+
+    sizes = CONFIG3_SIZES * pool_batches
+    frames, _ = scenes.render_many(3, sizes, threads=os.cpu_count() or 8)
+    dev = [torch.from_numpy(f).cuda() for f in frames]
+    nb = len(CONFIG3_SIZES)
+    sets = [dev[k * nb:(k + 1) * nb] for k in range(pool_batches)]
+    strides = [w for w, _ in CONFIG3_SIZES]
+    cams = [(w, h, FAMILIES) for w, h in CONFIG3_SIZES]
+    plans = [bdcudatag.Batch(cams) for _ in range(streams)]
+    default_launch = plans[0].launch()
+    best, tuned_ms = plans[0].autotune(sets[0], strides, iterations=10)
+    for p in plans[1:]:
+        p.set_launch(**best)
+    ts = [torch.cuda.Stream() for _ in range(streams)]
+    for p, st in zip(plans, ts):
+        p.set_stream(st)
+    elapsed, lat = run_batched(plans, ts, sets, steps, 5, device=True, strides=strides)
+    for p in plans:
+        p.set_stream(None)
+    found, out = plans[0].detect(sets[1], strides, device=True)
+    exact = True
+    for i in range(nb):
+        w, h = CONFIG3_SIZES[i]
+        for fam in (0, 1):
+            n, d = bdcudatag.Detector(fam, w, h).detect(frames[nb + i])
+            exact = exact and found[i, fam] == n and out[i, fam, :n].tobytes() == d.tobytes()
+    batch_bytes = sum(w * h for w, h in CONFIG3_SIZES)
+    return {"frames_per_s": round(steps * nb / (elapsed * 1e-3), 2), "batch_frames": nb,
+            "batch_bytes": batch_bytes, "streams": streams, "steps": steps,
+            "p50_ms": round(pct(lat, 50), 4), "p99_ms": round(pct(lat, 99), 4),
+            "tuned_launch": best, "default_launch": default_launch,
+            "tuned_batch_gpu_ms": round(tuned_ms, 4), "bit_exact_vs_single_frame": bool(exact)}
 
 
 def measure_serving(seconds: float, pool_per_cam: int = 12):
@@ -549,6 +595,7 @@ def bench_ours(args, rank, world, local_rank):
     cpu = measure_cpu_baseline(frames)
     serving = measure_serving(args.serving_seconds) if args.serving_seconds > 0 else None
     refine = measure_refine()
+    config3 = measure_config3(max(50, args.steps // 20))
     result_bytes = BATCH * ((32 + 2 * plans[0].max_detections * 84 + 255) // 256 * 256)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
@@ -571,6 +618,7 @@ def bench_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "serving": serving,
         "refine": refine,
+        "config3": config3,
         "clocks": clocks.summary(),
         "gpu_launches": 9 * args.steps,
     }

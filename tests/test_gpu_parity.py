@@ -249,3 +249,32 @@ def test_batch_pinned_stream_query_profile():
             n, want = oracle.Frame(frames[i], fam).detections()
             assert found[i, fam] == n
             same_records(out[i, fam, :n], want)
+
+
+def test_launch_shapes_and_autotune_keep_results():
+    torch = pytest.importorskip("torch")
+    sizes = [(640, 480), (1280, 800), (1600, 1304), (1920, 1080)] * 4
+    frames, _ = scenes.render_many(3, sizes, threads=8, base=scenes.base_seed(3) + 500)
+    dev = [torch.from_numpy(f).cuda() for f in frames]
+    strides = [w for w, _ in sizes]
+    batch = bdcudatag.Batch([(w, h, 3) for w, h in sizes])
+    found, out = batch.detect(dev, strides, device=True)
+    shapes = [dict(stats_rows=2), dict(stats_rows=4, fit_warps=4),
+              dict(fit_ctas_per_sm=2, decode_ctas_per_sm=2),
+              dict(stats_rows=1, fit_warps=8, fit_ctas_per_sm=16, decode_ctas_per_sm=8)]
+    for shape in shapes:
+        batch.set_launch(**shape)
+        f2, o2 = batch.detect(dev, strides, device=True)
+        assert np.array_equal(f2, found) and o2.tobytes() == out.tobytes(), shape
+    best, ms = batch.autotune(dev, strides, iterations=4)
+    assert ms > 0 and best["fit_warps"] in (4, 8)
+    f3, o3 = batch.detect(dev, strides, device=True)
+    assert np.array_equal(f3, found) and o3.tobytes() == out.tobytes()
+    with pytest.raises(RuntimeError):
+        batch.set_launch(stats_rows=3)
+    # the single-frame path agrees with the batch
+    for i in (0, 5, 10, 15):
+        w, h = sizes[i]
+        for fam in (0, 1):
+            n, d = bdcudatag.Detector(fam, w, h).detect(frames[i])
+            assert found[i, fam] == n and out[i, fam, :n].tobytes() == d.tobytes()
