@@ -16,3 +16,20 @@ mkdir -p "$HERE/_ref"
 g++ -O2 -std=c++20 -I"$REF/detector/src" -I"$REF/detector/tests" \
     "$REF/detector/bench/scene_gen.cpp" -o "$HERE/_ref/bdcudatag_scenes"
 echo "built $HERE/_ref/bdcudatag_scenes"
+
+# The reference's own C++ consumers -- its known-answer test program and its
+# benchmark -- compiled unchanged from where they lie, against this project's
+# public headers and linked to this project's libbdcudatag.so.  The binaries
+# are x86 and need a GPU, so they serve as a link-level drop-in check here.
+LIB_DIR="$HERE/../bd-cudatag_gb300"
+if [ -f "$LIB_DIR/libbdcudatag.so" ]; then
+    CUDA_INC=/usr/local/cuda/include
+    CUDA_LIB=/usr/local/cuda/lib64
+    for prog in tests/test_detector.cpp bench/bench_detector.cpp; do
+        out="$HERE/_ref/$(basename "${prog%.cpp}")_on_gb300"
+        g++ -O2 -std=c++20 -I"$HERE/../include" -I"$REF/detector/src" -I"$REF/detector/tests" \
+            -I"$CUDA_INC" "$REF/detector/$prog" -o "$out" \
+            -L"$LIB_DIR" -lbdcudatag -L"$CUDA_LIB" -lcudart -lpthread -Wl,-rpath,"$LIB_DIR"
+        echo "built $out"
+    done
+fi
