@@ -633,50 +633,69 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
 //    row of the band above; every row of a fallback band (the reference's
 //    k_merge_runs :509-557 rules).
 // ===========================================================================
+__device__ __forceinline__ void merge_run_with_row_above(uint32_t* parent, const uint32_t* cur,
+                                                         const uint32_t* prev, int i, int prev_n,
+                                                         uint32_t cur_base, uint32_t prev_base,
+                                                         bool same_row) {
+    const uint32_t run = cur[i];
+    const int x0 = static_cast<int>(run & 0xffffu);
+    const int x1 = static_cast<int>(run >> 16);
+    if (same_row && i > 0) {
+        const int px1 = static_cast<int>(cur[i - 1] >> 16);
+        if (px1 + 1 >= x0) uf_union(parent, cur_base + i, cur_base + i - 1);
+    }
+    if (prev_n == 0) return;
+    int lo = 0, hi = prev_n - 1, first = prev_n;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        if (static_cast<int>(prev[mid] >> 16) >= x0 - 1) {
+            first = mid;
+            hi = mid - 1;
+        } else {
+            lo = mid + 1;
+        }
+    }
+    for (int k = first; k < prev_n; ++k) {
+        const int px0 = static_cast<int>(prev[k] & 0xffffu);
+        if (px0 > x1 + 1) break;
+        uf_union(parent, cur_base + i, prev_base + k);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b,
                                                const FrameIO* __restrict__ io) {
     const int fi = frame_of_band(b, blockIdx.x);
     if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
+    const int row_cap = d.row_cap;
+    uint32_t* parent = d.parent;
+    if (d.band_mode[ty] == 0) {
+        // Band-local unions are done: only the first row meets the band
+        // above; its runs are spread over the whole CTA.
+        const int y = ty * kTile;
+        if (y <= 0) return;
+        const int n = static_cast<int>(d.row_count[y]);
+        const int prev_n = static_cast<int>(d.row_count[y - 1]);
+        const uint32_t* cur = d.runs + static_cast<int64_t>(y) * row_cap;
+        const uint32_t* prev = d.runs + static_cast<int64_t>(y - 1) * row_cap;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            merge_run_with_row_above(parent, cur, prev, i, prev_n, static_cast<uint32_t>(y * row_cap),
+                                     static_cast<uint32_t>((y - 1) * row_cap), false);
+        }
+        return;
+    }
+    // Fallback band: every row, one warp per row.
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int y = ty * kTile + w;
     if (y <= 0 || y >= d.height) return;
-    const bool full = d.band_mode[ty] != 0;
-    if (!full && w != 0) return;
     const int n = static_cast<int>(d.row_count[y]);
-    if (n == 0) return;
-    const int row_cap = d.row_cap;
     const int prev_n = static_cast<int>(d.row_count[y - 1]);
     const uint32_t* cur = d.runs + static_cast<int64_t>(y) * row_cap;
     const uint32_t* prev = d.runs + static_cast<int64_t>(y - 1) * row_cap;
-    const uint32_t cur_base = static_cast<uint32_t>(y * row_cap);
-    const uint32_t prev_base = static_cast<uint32_t>((y - 1) * row_cap);
-    uint32_t* parent = d.parent;
     for (int i = lane; i < n; i += 32) {
-        const uint32_t run = cur[i];
-        const int x0 = static_cast<int>(run & 0xffffu);
-        const int x1 = static_cast<int>(run >> 16);
-        if (full && i > 0) {
-            const int px1 = static_cast<int>(cur[i - 1] >> 16);
-            if (px1 + 1 >= x0) uf_union(parent, cur_base + i, cur_base + i - 1);
-        }
-        if (prev_n == 0) continue;
-        int lo = 0, hi = prev_n - 1, first = prev_n;
-        while (lo <= hi) {
-            const int mid = (lo + hi) >> 1;
-            if (static_cast<int>(prev[mid] >> 16) >= x0 - 1) {
-                first = mid;
-                hi = mid - 1;
-            } else {
-                lo = mid + 1;
-            }
-        }
-        for (int k = first; k < prev_n; ++k) {
-            const int px0 = static_cast<int>(prev[k] & 0xffffu);
-            if (px0 > x1 + 1) break;
-            uf_union(parent, cur_base + i, prev_base + k);
-        }
+        merge_run_with_row_above(parent, cur, prev, i, prev_n, static_cast<uint32_t>(y * row_cap),
+                                 static_cast<uint32_t>((y - 1) * row_cap), true);
     }
 }
 
@@ -697,6 +716,7 @@ __global__ void __launch_bounds__(256) k_region_stats(const BatchDesc* __restric
         const uint32_t s = list[k];
         const uint32_t g = uf_find(d.parent, s);
         if (g == s) continue;
+        d.parent[s] = g;  // later label walks take two hops
         const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[s];
         atomicAdd(&d.area[g], d.area[s]);
         atomicMin(&d.bbox[g * 4 + 0], bb.x);
@@ -729,9 +749,21 @@ __device__ __forceinline__ int candidate_bin(const FrameDesc& d, uint32_t idx) {
     return 63 - min(log2_area, 63);
 }
 
+__device__ __forceinline__ uint32_t band_slot(const uint32_t* rowoff, int y0, uint32_t row_cap,
+                                              uint32_t i) {
+    int row = 0;
+    while (row + 1 < kTile && rowoff[row + 1] <= i) ++row;
+    return static_cast<uint32_t>(y0 + row) * row_cap + (i - rowoff[row]);
+}
+
+// One CTA per band, 256 runs at a time in slot order: root labels, the
+// tag-like filter, and each candidate's rank among the band's candidates
+// of its area bin.
 __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict__ b,
                                                     const FrameIO* __restrict__ io) {
-    __shared__ uint32_t s_rowbin[kTile][64];
+    __shared__ uint32_t s_rowoff[kTile + 1];
+    __shared__ uint32_t s_wbin[8][64];
+    __shared__ uint32_t s_run[64];
     __shared__ uint32_t s_chunk[32][64];
     __shared__ uint32_t s_total[64];
     __shared__ int s_last;
@@ -742,56 +774,55 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
     FrameState* st = d.state;
-    for (int i = tid; i < kTile * 64; i += blockDim.x) (&s_rowbin[0][0])[i] = 0;
+    const int y0 = ty * kTile;
+    const uint32_t row_cap = static_cast<uint32_t>(d.row_cap);
+    if (tid == 0) {
+        uint32_t off = 0;
+        for (int r = 0; r < kTile; ++r) {
+            s_rowoff[r] = off;
+            off += y0 + r < d.height ? d.row_count[y0 + r] : 0u;
+        }
+        s_rowoff[kTile] = off;
+    }
+    if (tid < 64) s_run[tid] = 0;
     __syncthreads();
-
+    const uint32_t total = s_rowoff[kTile];
     const int w = tid >> 5, lane = tid & 31;
-    const int y = ty * kTile + w;
-    const int n = y < d.height ? static_cast<int>(d.row_count[y]) : 0;
-    const uint32_t base = static_cast<uint32_t>(y * d.row_cap);
-    for (int c = 0; c < n; c += 32) {
-        const int i = c + lane;
+    for (uint32_t base = 0; base < total; base += blockDim.x) {
+        const uint32_t i = base + tid;
         int bin = -1;
-        uint32_t idx = 0;
-        if (i < n) {
-            idx = base + static_cast<uint32_t>(i);
-            const uint32_t root = uf_root_readonly(d.parent, idx);
-            d.parent[idx] = root;
-            if (root == idx) bin = candidate_bin(d, idx);
+        uint32_t slot = 0;
+        if (i < total) {
+            slot = band_slot(s_rowoff, y0, row_cap, i);
+            const uint32_t root = uf_root_readonly(d.parent, slot);
+            d.parent[slot] = root;
+            if (root == slot) bin = candidate_bin(d, slot);
         }
         const uint32_t key = bin >= 0 ? static_cast<uint32_t>(bin) : 64u + lane;
         const uint32_t peers = __match_any_sync(kFull, key);
+        const uint32_t rank = __popc(peers & lanemask_lt());
+        s_wbin[w][lane] = 0;
+        s_wbin[w][lane + 32] = 0;
+        __syncthreads();
+        if (bin >= 0 && rank == 0) s_wbin[w][bin] = __popc(peers);
+        __syncthreads();
         uint32_t meta = kNone;
-        uint32_t rank = 0;
         if (bin >= 0) {
-            rank = __popc(peers & lanemask_lt());
-            meta = (static_cast<uint32_t>(bin) << 24) | (s_rowbin[w][bin] + rank);
+            uint32_t pos = s_run[bin] + rank;
+            for (int w2 = 0; w2 < w; ++w2) pos += s_wbin[w2][bin];
+            meta = (static_cast<uint32_t>(bin) << 24) | pos;
         }
-        __syncwarp();
-        if (bin >= 0 && rank == 0) s_rowbin[w][bin] += __popc(peers);
-        __syncwarp();
-        if (i < n) d.cand_meta[idx] = meta;
+        __syncthreads();
+        if (tid < 64) {
+            uint32_t add = 0;
+            for (int w2 = 0; w2 < 8; ++w2) add += s_wbin[w2][tid];
+            s_run[tid] += add;
+        }
+        if (i < total) d.cand_meta[slot] = meta;
+        __syncthreads();  // s_wbin is cleared for the next chunk
     }
     __syncthreads();
-    // Exclusive prefix over the band's rows per bin; band totals.
-    if (tid < 64) {
-        uint32_t run = 0;
-        for (int r = 0; r < kTile; ++r) {
-            const uint32_t v = s_rowbin[r][tid];
-            s_rowbin[r][tid] = run;
-            run += v;
-        }
-        d.band_bins[ty * 64 + tid] = run;
-    }
-    __syncthreads();
-    for (int c = 0; c < n; c += 32) {
-        const int i = c + lane;
-        if (i < n) {
-            const uint32_t idx = base + static_cast<uint32_t>(i);
-            const uint32_t meta = d.cand_meta[idx];
-            if (meta != kNone) d.cand_meta[idx] = meta + s_rowbin[w][meta >> 24];
-        }
-    }
+    if (tid < 64) d.band_bins[ty * 64 + tid] = s_run[tid];
     __threadfence();
     __syncthreads();
     if (tid == 0) s_last = atomicAdd(&st->done_cands, 1u) == static_cast<uint32_t>(d.tile_h - 1);
@@ -840,24 +871,32 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_cand_emit(const BatchDesc* __restrict__ b,
                                                    const FrameIO* __restrict__ io) {
+    __shared__ uint32_t s_rowoff[kTile + 1];
     const int fi = frame_of_band(b, blockIdx.x);
     if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
     const int ty = blockIdx.x - b->band_prefix[fi];
     const FrameState* st = d.state;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int y = ty * kTile + w;
-    if (y >= d.height) return;
-    const int n = static_cast<int>(d.row_count[y]);
+    const int y0 = ty * kTile;
+    const uint32_t row_cap = static_cast<uint32_t>(d.row_cap);
+    if (threadIdx.x == 0) {
+        uint32_t off = 0;
+        for (int r = 0; r < kTile; ++r) {
+            s_rowoff[r] = off;
+            off += y0 + r < d.height ? d.row_count[y0 + r] : 0u;
+        }
+        s_rowoff[kTile] = off;
+    }
+    __syncthreads();
+    const uint32_t total = s_rowoff[kTile];
     const uint32_t limit = st->n_candidates;
-    const uint32_t base = static_cast<uint32_t>(y * d.row_cap);
-    for (int i = lane; i < n; i += 32) {
-        const uint32_t idx = base + static_cast<uint32_t>(i);
-        const uint32_t meta = d.cand_meta[idx];
+    for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
+        const uint32_t slot = band_slot(s_rowoff, y0, row_cap, i);
+        const uint32_t meta = d.cand_meta[slot];
         if (meta == kNone) continue;
         const uint32_t bin = meta >> 24;
         const uint32_t pos = st->bin_base[bin] + d.band_bins[ty * 64 + bin] + (meta & 0xffffffu);
-        if (pos < limit) d.candidates[pos] = idx;
+        if (pos < limit) d.candidates[pos] = slot;
     }
 }
 
