@@ -115,7 +115,7 @@ GB300_SYMBOLS = [
     "bd_server_create", "bd_server_destroy", "bd_server_submit", "bd_server_wait",
     "bd_server_poll", "bd_server_get_stats",
     "bd_tag_template", "bd_refine_forward", "bd_refine_backward", "bd_refine_gauss_newton",
-    "bd_batch_get_launch", "bd_batch_set_launch", "bd_batch_autotune",
+    "bd_batch_get_launch", "bd_batch_set_launch", "bd_batch_autotune", "bd_batch_pipeline",
 ]
 
 _LIB = None
@@ -194,6 +194,9 @@ def lib() -> ctypes.CDLL:
         L.bd_batch_autotune.argtypes = [_P, _P, _P, ctypes.c_int32, ctypes.POINTER(LaunchConfig),
                                         ctypes.POINTER(ctypes.c_float)]
         L.bd_batch_autotune.restype = ctypes.c_int32
+        L.bd_batch_pipeline.argtypes = [_P, ctypes.c_int32, _P, _P, ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_int32, _P, ctypes.POINTER(ctypes.c_double)]
+        L.bd_batch_pipeline.restype = ctypes.c_int32
         L.bd_tag_template.argtypes = [ctypes.c_int32, ctypes.c_int32, _P]
         L.bd_tag_template.restype = ctypes.c_int32
         L.bd_refine_forward.argtypes = [ctypes.POINTER(RefineArgs), _P, _P, _P]
@@ -484,3 +487,21 @@ def refine_args(images, corners, templates, image_index=None, levels=None,
                       corners.data_ptr(), templates.data_ptr(),
                       levels.data_ptr() if levels is not None else None, templates.shape[-1],
                       samples_per_cell)
+
+
+def pipeline(batches: list, frame_sets: list, strides, steps: int, device: bool = True):
+    """Runs `steps` batches round-robin over `batches` in native code.
+    frame_sets: list of per-camera frame lists.  Returns (wall ms, per-batch
+    latency ms array)."""
+    cams = len(frame_sets[0])
+    handles = (ctypes.c_void_p * len(batches))(*[b.handle for b in batches])
+    flat = (ctypes.c_void_p * (cams * len(frame_sets)))(*[_ptr(f) for fs in frame_sets for f in fs])
+    st = np.asarray(strides, dtype=np.int32)
+    lat = np.zeros(max(steps, 1), dtype=np.float32)
+    wall = ctypes.c_double(0.0)
+    rc = lib().bd_batch_pipeline(ctypes.cast(handles, _P), len(batches), ctypes.cast(flat, _P),
+                                 st.ctypes.data, len(frame_sets), steps, 1 if device else 0,
+                                 lat.ctypes.data, ctypes.byref(wall))
+    if rc != 0:
+        raise RuntimeError(f"pipeline failed ({rc}): {last_error()}")
+    return wall.value, lat[:steps]

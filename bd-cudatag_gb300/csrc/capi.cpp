@@ -439,6 +439,76 @@ int32_t bd_batch_detect_device(bd_batch* batch, const uint8_t* const* frames,
     return bd_batch_wait(batch, out, found);
 }
 
+int32_t bd_batch_pipeline(bd_batch* const* batches, int32_t count, const uint8_t* const* frames,
+                          const int32_t* strides, int32_t sets, int32_t steps, int32_t device,
+                          float* latency_ms, double* wall_ms) {
+    if (!batches || count < 1 || !frames || !strides || sets < 1 || steps < 0) {
+        set_error("bd_batch_pipeline: bad arguments");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    const int cams = batches[0] ? batches[0]->plan->frames() : 0;
+    for (int i = 0; i < count; ++i) {
+        if (!batches[i] || batches[i]->plan->frames() != cams) {
+            set_error("bd_batch_pipeline: batches must be non-null with the same cameras");
+            return BD_ERROR_INVALID_ARGUMENT;
+        }
+    }
+    std::vector<bool> busy(count, false);
+    std::vector<int> step_of(count, -1);
+    std::vector<Clock::time_point> issued(count);
+    std::string error;
+    auto finish_one = [&](int i) -> bool {
+        bdgb::Plan& plan = *batches[i]->plan;
+        if (plan.wait(&error) != 0) return false;
+        if (latency_ms) {
+            latency_ms[step_of[i]] =
+                std::chrono::duration<float, std::milli>(Clock::now() - issued[i]).count();
+        }
+        busy[i] = false;
+        return true;
+    };
+    const auto t0 = Clock::now();
+    for (int k = 0; k < steps; ++k) {
+        const int i = k % count;
+        while (busy[i]) {
+            // Poll every batch in flight so completions are stamped on time.
+            for (int j = 0; j < count; ++j) {
+                if (!busy[j]) continue;
+                const int q = batches[j]->plan->query(&error);
+                if (q < 0 || (q == 1 && !finish_one(j))) {
+                    set_error(error);
+                    return BD_ERROR_CUDA;
+                }
+            }
+        }
+        const uint8_t* const* set = frames + static_cast<size_t>(k % sets) * cams;
+        issued[i] = Clock::now();
+        step_of[i] = k;
+        bdgb::Plan& plan = *batches[i]->plan;
+        const int rc = device ? plan.submit_device(set, strides, &error)
+                              : plan.submit_host(set, strides, &error);
+        if (rc != 0) {
+            set_error(error);
+            return BD_ERROR_CUDA;
+        }
+        busy[i] = true;
+    }
+    for (int i = 0; i < count; ++i) {
+        while (busy[i]) {
+            for (int j = 0; j < count; ++j) {
+                if (!busy[j]) continue;
+                const int q = batches[j]->plan->query(&error);
+                if (q < 0 || (q == 1 && !finish_one(j))) {
+                    set_error(error);
+                    return BD_ERROR_CUDA;
+                }
+            }
+        }
+    }
+    if (wall_ms) *wall_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+    return BD_OK;
+}
+
 int32_t bd_batch_set_stream(bd_batch* batch, void* cuda_stream) {
     if (!batch) {
         set_error("null batch");

@@ -119,54 +119,29 @@ def pct(values, q):
 
 
 def run_batched(plans, streams, frame_sets, steps, warmup, device: bool, strides=None):
-    """Round-robin batches over the plans; returns (elapsed ms by CUDA
-    events, per-batch latencies in ms)."""
+    """Round-robin batches over the plans in native code
+    (bd_batch_pipeline); returns (elapsed ms by CUDA events, per-batch
+    latencies in ms, submit to completion on the host)."""
     import torch
 
-    S = len(plans)
-    issued = {}  # plan index -> submit time
+    import bdcudatag
 
-    def drain(i, lat):
-        if i in issued:
-            plans[i].wait(copy=False)
-            if lat is not None:
-                lat.append((time.perf_counter() - issued[i]) * 1e3)
-            del issued[i]
-
-    def loop(n, lat, offset):
-        for k in range(n):
-            i = k % S
-            if i in issued:
-                # Poll every plan in flight so completions are stamped when
-                # they happen, not when their slot is reused.
-                while not plans[i].query():
-                    for j in list(issued):
-                        if j != i and plans[j].query():
-                            drain(j, lat)
-                drain(i, lat)
-            frames = frame_sets[(offset + k) % len(frame_sets)]
-            issued[i] = time.perf_counter()
-            plans[i].submit(frames, strides or [W] * BATCH, device=device)
-        for i in list(issued):
-            while not plans[i].query():
-                pass
-            drain(i, lat)
-
-    loop(warmup, None, 0)
+    st = strides or [W] * BATCH
+    if warmup:
+        bdcudatag.pipeline(plans, frame_sets, st, warmup, device)
     torch.cuda.synchronize()
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
-    lat: list[float] = []
     main = torch.cuda.current_stream()
     start.record(main)
-    for st in streams:
-        st.wait_event(start)
-    loop(steps, lat, warmup)
-    for st in streams:
-        main.wait_stream(st)
+    for s in streams:
+        s.wait_event(start)
+    _, lat = bdcudatag.pipeline(plans, frame_sets, st, steps, device)
+    for s in streams:
+        main.wait_stream(s)
     stop.record(main)
     torch.cuda.synchronize()
-    return start.elapsed_time(stop), lat
+    return start.elapsed_time(stop), list(lat)
 
 
 def tune_throughput(plans, streams, frame_sets, steps=400, strides=None):

@@ -113,6 +113,22 @@ BD_API const char* bd_stage_name(int32_t stage);
 BD_API int32_t bd_batch_profile_device(bd_batch* batch, const uint8_t* const* frames,
                                        const int32_t* strides, float* stage_ms);
 
+/*
+ * Pipelined run of many batches from native code: `steps` batches go round-
+ * robin over the `count` bd_batch objects (each keeps its own stream, see
+ * bd_batch_set_stream), so up to `count` run on the GPU at once.  Batch k
+ * uses frame set k % sets: frames[(k % sets) * cameras + i] is camera i's
+ * frame (device pointers when device != 0, else host), strides[i] its stride.
+ * All batches must have the same cameras.  Results stay in each batch (read
+ * them with bd_batch_wait after the last step if needed).  latency_ms (steps
+ * entries, or NULL) receives submit-to-completion time per batch; wall_ms
+ * the host time of the whole run.
+ */
+BD_API int32_t bd_batch_pipeline(bd_batch* const* batches, int32_t count,
+                                 const uint8_t* const* frames, const int32_t* strides,
+                                 int32_t sets, int32_t steps, int32_t device, float* latency_ms,
+                                 double* wall_ms);
+
 /* Pinned host staging buffer of camera i (width * height bytes, stride =
  * width).  A frame written here is submitted without the staging copy by
  * passing this pointer as frames[i]. */
