@@ -566,9 +566,12 @@ def bench_ours(args, rank, world, local_rank):
 
     if world > 1:
         torch.distributed.barrier()
+    tuned, tune_trials = None, None
+    if args.tune or not args.quick:
+        # Launch shapes scored on frames/s with all streams busy (untimed).
+        tuned, tune_trials = tune_throughput(plans, streams, sets_dev)
     if args.quick:
-        if args.tune:
-            tuned, _ = tune_throughput(plans, streams, sets_dev)
+        if tuned:
             print(json.dumps({"tuned": tuned}), flush=True)
         elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps, args.warmup, device=True)
         if rank == 0:
