@@ -83,8 +83,8 @@ class RefineArgs(ctypes.Structure):
 
 
 class LaunchConfig(ctypes.Structure):
-    _fields_ = [("stats_rows", ctypes.c_int32), ("fit_warps", ctypes.c_int32),
-                ("fit_ctas_per_sm", ctypes.c_int32), ("decode_ctas_per_sm", ctypes.c_int32)]
+    _fields_ = [("stats_rows", ctypes.c_int32), ("quad_warps", ctypes.c_int32),
+                ("quad_ctas_per_sm", ctypes.c_int32), ("quad_split", ctypes.c_int32)]
 
 
 class Camera(ctypes.Structure):

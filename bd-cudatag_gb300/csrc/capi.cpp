@@ -523,9 +523,9 @@ int32_t bd_batch_get_launch(const bd_batch* batch, bd_launch_config* out) {
     if (!batch || !out) return BD_ERROR_INVALID_ARGUMENT;
     const bdgb::LaunchConfig& lc = batch->plan->launch();
     out->stats_rows = lc.stats_rows;
-    out->fit_warps = lc.fit_warps;
-    out->fit_ctas_per_sm = lc.fit_ctas_per_sm;
-    out->decode_ctas_per_sm = lc.decode_ctas_per_sm;
+    out->quad_warps = lc.quad_warps;
+    out->quad_ctas_per_sm = lc.quad_ctas_per_sm;
+    out->quad_split = lc.quad_split;
     return BD_OK;
 }
 
@@ -536,9 +536,9 @@ int32_t bd_batch_set_launch(bd_batch* batch, const bd_launch_config* launch) {
     }
     bdgb::LaunchConfig lc;
     lc.stats_rows = launch->stats_rows;
-    lc.fit_warps = launch->fit_warps;
-    lc.fit_ctas_per_sm = launch->fit_ctas_per_sm;
-    lc.decode_ctas_per_sm = launch->decode_ctas_per_sm;
+    lc.quad_warps = launch->quad_warps;
+    lc.quad_ctas_per_sm = launch->quad_ctas_per_sm;
+    lc.quad_split = launch->quad_split;
     const std::lock_guard<std::mutex> lock(batch->plan->mutex());
     std::string error;
     if (batch->plan->set_launch(lc, &error) != 0) {

@@ -63,6 +63,9 @@ int auto_max_candidates(int width, int height, int configured) {
 struct Plan::Impl {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t branch = nullptr;      // parallel branch: big-candidate kernel
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join = nullptr;
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev_stop = nullptr;
     void* arena = nullptr;
@@ -99,6 +102,10 @@ struct Plan::Impl {
         for (cudaEvent_t e : stage_events) {
             if (e) cudaEventDestroy(e);
         }
+        if (branch) cudaStreamSynchronize(branch);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (branch) cudaStreamDestroy(branch);
         if (ev_start) cudaEventDestroy(ev_start);
         if (ev_stop) cudaEventDestroy(ev_stop);
         if (stream) cudaStreamDestroy(stream);
@@ -118,8 +125,9 @@ struct Plan::Impl {
                             cudaMemcpyHostToDevice, s);
         }
         cudaMemsetAsync(states, 0, states_bytes, s);
+        const ForkJoin fork{branch, ev_fork, ev_join};
         enqueue_pipeline(dev_desc, host_desc, mode == 2 ? io_caller : io_fixed, s, launch_cfg, sm_count,
-                         events);
+                         branch ? &fork : nullptr, events);
         cudaMemcpyAsync(results_pinned, results_dev, results_bytes, cudaMemcpyDeviceToHost, s);
     }
 
@@ -339,6 +347,9 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     }
     std::memset(im.results_pinned, 0, im.results_bytes);
     st = cudaStreamCreateWithFlags(&im.stream, cudaStreamNonBlocking);
+    if (st == cudaSuccess) st = cudaStreamCreateWithFlags(&im.branch, cudaStreamNonBlocking);
+    if (st == cudaSuccess) st = cudaEventCreateWithFlags(&im.ev_fork, cudaEventDisableTiming);
+    if (st == cudaSuccess) st = cudaEventCreateWithFlags(&im.ev_join, cudaEventDisableTiming);
     if (st == cudaSuccess) st = cudaEventCreate(&im.ev_start);
     if (st == cudaSuccess) st = cudaEventCreate(&im.ev_stop);
     if (st != cudaSuccess) return fail(cuda_error("cudaStreamCreate", st));
@@ -504,8 +515,9 @@ const LaunchConfig& Plan::launch() const { return impl_->launch_cfg; }
 int Plan::set_launch(const LaunchConfig& lc, std::string* error) {
     Impl& im = *impl_;
     if (!(lc.stats_rows == 1 || lc.stats_rows == 2 || lc.stats_rows == 4) ||
-        !(lc.fit_warps == 4 || lc.fit_warps == 8) || lc.fit_ctas_per_sm < 1 ||
-        lc.fit_ctas_per_sm > 32 || lc.decode_ctas_per_sm < 1 || lc.decode_ctas_per_sm > 32) {
+        !(lc.quad_warps == 2 || lc.quad_warps == 4 || lc.quad_warps == kMaxQuadWarps) ||
+        lc.quad_ctas_per_sm < 1 || lc.quad_ctas_per_sm > 32 || lc.quad_split < 0 ||
+        lc.quad_split > 4096) {
         if (error) *error = "launch config out of range";
         return -1;
     }
@@ -546,9 +558,9 @@ int Plan::autotune(const uint8_t* const* frames, const int32_t* strides, int ite
     float best_t = 0.0f;
     if (measure(best, &best_t) != 0) return -1;
     const int stats_rows[] = {1, 2, 4};
-    const int fit_warps[] = {8, 4};
-    const int fit_ctas[] = {2, 4, 8, 16};
-    const int dec_ctas[] = {2, 4, 6, 8};
+    const int quad_warps[] = {2, 4, 8};
+    const int quad_ctas[] = {2, 4, 8, 16};
+    const int quad_split[] = {32, 48, 64, 96, 0};
     auto try_values = [&](auto field, const int* values, int n) -> int {
         for (int i = 0; i < n; ++i) {
             LaunchConfig lc = best;
@@ -564,9 +576,9 @@ int Plan::autotune(const uint8_t* const* frames, const int32_t* strides, int ite
         return 0;
     };
     if (try_values(&LaunchConfig::stats_rows, stats_rows, 3) != 0) return -1;
-    if (try_values(&LaunchConfig::fit_warps, fit_warps, 2) != 0) return -1;
-    if (try_values(&LaunchConfig::fit_ctas_per_sm, fit_ctas, 4) != 0) return -1;
-    if (try_values(&LaunchConfig::decode_ctas_per_sm, dec_ctas, 4) != 0) return -1;
+    if (try_values(&LaunchConfig::quad_warps, quad_warps, 3) != 0) return -1;
+    if (try_values(&LaunchConfig::quad_ctas_per_sm, quad_ctas, 4) != 0) return -1;
+    if (try_values(&LaunchConfig::quad_split, quad_split, 5) != 0) return -1;
     if (set_launch(best, error) != 0) return -1;
     if (best_ms) *best_ms = best_t;
     return 0;

@@ -15,10 +15,9 @@
 //   k_cand_count     root flattening, tag-like filter, ordered per-band
 //                    bin ranks, (last CTA) bin bases <- k_collect_candidates :591
 //   k_cand_emit      ordered flattening into candidates  <- k_order_candidates :642
-//   k_fit            hull, four corners, per-family edge refinement
-//                    <- k_fit_quads :1081
-//   k_decode         8 variants per candidate, warp per variant
-//                    <- k_decode_quads :1438
+//   k_fit_decode     warp per candidate: hull, four corners, per-family
+//                    edge refinement and decode  <- k_fit_quads :1081,
+//                    k_decode_quads :1438
 //   k_finalize       de-duplication, sort by id, FP64 homography
 //                    <- k_finalize :1542, host fill_homography :1739
 //
@@ -1049,12 +1048,6 @@ __device__ __forceinline__ bool intersect_lines(const float li[4], const float l
     return true;
 }
 
-// One warp fits one edge (reference fit_edge_line_warp :881-1016).  Sample
-// s (< 16) along the edge is probed by lanes s and s + 16, which take the
-// even and odd probe steps and leave the profile in shared memory; lane s
-// then picks the peak exactly as the reference lane does.  The moments sit
-// in lanes 0..15 (zero above), so the shuffle tree sums them in the
-// reference's order.
 // Bilinear sample with the reference's bounds rule (sample_bilinear
 // :833-849): -1 outside [0, width-1) x [0, height-1).  The address is
 // clamped and the result selected instead of branching, so the loads of
@@ -1089,6 +1082,215 @@ __device__ __forceinline__ float rise_ro(const uint8_t* __restrict__ image, int 
 
 constexpr int kMaxProbes = kFitProbeHalf * 2 + 1;
 
+// The four edge lines of one quad, fitted by one warp (reference
+// fit_edge_line_warp :881-1016, which spends a warp per edge).  Lane l takes
+// sample l % seg of edge base + l / seg, with seg = 8 when no edge has more
+// than 8 samples (all four edges in one round) and 16 otherwise (two rounds
+// of two edges).  A lane probes its whole profile into its own shared-memory
+// row (kMaxProbes floats; the row stride is odd, so rows fall in different
+// banks) and picks the peak exactly as the reference lane does.  An edge's
+// moments are summed by a seg-lane shuffle tree: the reference sums them
+// with a 32-lane tree over samples 0..15 and zeros above, whose first one
+// (seg 16) or two (seg 8) levels only add +0.0, so adding +0.0 that many
+// times and finishing within the segment gives the same bits.  Segment
+// leaders fit the lines into lines[edge] / have[edge].
+__device__ void fit_edges_warp(const float (*q)[2], const uint8_t* __restrict__ image, int width,
+                               int height, int64_t stride, int dim, bool first_pass, int lane,
+                               float* s_mags, float (*lines)[4], int* have) {
+    int my_samples = 0;
+    if (lane < 4) {
+        const int bi = (lane + 1) & 3;
+        const float ex = q[bi][0] - q[lane][0];
+        const float ey = q[bi][1] - q[lane][1];
+        const float len = sqrtf(ex * ex + ey * ey);
+        if (len >= 8.0f) my_samples = min(max(static_cast<int>(len / 6.0f), 8), 16);
+    }
+    const int seg = __reduce_max_sync(kFull, static_cast<unsigned>(my_samples)) <= 8 ? 8 : 16;
+    float* mags = s_mags + lane * kMaxProbes;
+    for (int base = 0; base < 4; base += 32 / seg) {
+        const int edge = base + lane / seg;
+        const int sample = lane & (seg - 1);
+        const int bi = (edge + 1) & 3;
+        const float ax = q[edge][0], ay = q[edge][1];
+        const float ex = q[bi][0] - ax;
+        const float ey = q[bi][1] - ay;
+        const float len = sqrtf(ex * ex + ey * ey);
+        const bool edge_ok = len >= 8.0f;
+        float mx = 0.0f, my = 0.0f, mxx = 0.0f, mxy = 0.0f, myy = 0.0f;
+        int used = 0;
+        if (edge_ok) {
+            const float nx = ey / len;
+            const float ny = -ex / len;
+            const float cell = len / static_cast<float>(dim);
+            const float range = first_pass ? fminf(fmaxf(1.15f * cell, 1.5f), 2.5f * cell)
+                                           : fminf(fmaxf(0.30f * cell, 0.8f), 2.0f);
+            const int half = min(max(2, static_cast<int>(ceilf(range / 0.75f))), kFitProbeHalf);
+            const int probes = 2 * half + 1;
+            const float step = range / static_cast<float>(half);
+            const int samples = min(max(static_cast<int>(len / 6.0f), 8), 16);
+            if (sample < samples) {
+                const float alpha = static_cast<float>(sample + 1) / static_cast<float>(samples + 1);
+                const float px = ax + alpha * ex;
+                const float py = ay + alpha * ey;
+                float best_mag = 0.0f;
+                int best = -1;
+                // Four independent rises per block (indices past the end
+                // repeat the last probe and are dropped), then the
+                // reference's in-order peak scan over the block.
+                for (int i0 = 0; i0 < probes; i0 += 4) {
+                    float m[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int i = min(i0 + j, probes - 1);
+                        const float t = step * static_cast<float>(i - half);
+                        m[j] = rise_ro(image, width, height, stride, px + nx * t, py + ny * t, nx, ny);
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        if (i0 + j >= probes) break;
+                        mags[i0 + j] = m[j];
+                        if (m[j] > best_mag) {
+                            best_mag = m[j];
+                            best = i0 + j;
+                        }
+                    }
+                }
+                if (first_pass && best > 2) {
+                    const float accept = 0.70f * best_mag;
+                    for (int i = 1; i + 1 < best; ++i) {
+                        if (mags[i] < accept || mags[i] < mags[i - 1] || mags[i] < mags[i + 1]) continue;
+                        float valley = FLT_MAX;
+                        for (int k = i + 1; k < best; ++k) valley = fminf(valley, mags[k]);
+                        if (valley < 0.5f * mags[i]) {
+                            best = i;
+                            best_mag = mags[i];
+                            break;
+                        }
+                    }
+                }
+                if (best >= 0 && best_mag >= 6.0f) {
+                    float t = step * static_cast<float>(best - half);
+                    if (best > 0 && best < probes - 1) {
+                        const float m0 = rise_ro(image, width, height, stride, px + nx * (t - step),
+                                                 py + ny * (t - step), nx, ny);
+                        const float m2 = rise_ro(image, width, height, stride, px + nx * (t + step),
+                                                 py + ny * (t + step), nx, ny);
+                        const float den = m0 - 2.0f * best_mag + m2;
+                        if (den < -1e-3f) t += fminf(fmaxf(0.5f * (m0 - m2) / den, -0.5f), 0.5f) * step;
+                    }
+                    const float x = px + nx * t;
+                    const float y = py + ny * t;
+                    mx = x;
+                    my = y;
+                    mxx = x * x;
+                    mxy = x * y;
+                    myy = y * y;
+                    used = 1;
+                }
+            }
+        }
+        // Levels of the reference tree that only add the zero lanes.
+        for (int z = seg; z < 32; z <<= 1) {
+            mx = mx + 0.0f;
+            my = my + 0.0f;
+            mxx = mxx + 0.0f;
+            mxy = mxy + 0.0f;
+            myy = myy + 0.0f;
+        }
+        for (int off = seg >> 1; off > 0; off >>= 1) {
+            mx += __shfl_down_sync(kFull, mx, off, seg);
+            my += __shfl_down_sync(kFull, my, off, seg);
+            mxx += __shfl_down_sync(kFull, mxx, off, seg);
+            mxy += __shfl_down_sync(kFull, mxy, off, seg);
+            myy += __shfl_down_sync(kFull, myy, off, seg);
+            used += __shfl_down_sync(kFull, used, off, seg);
+        }
+        if (sample == 0) {
+            int ok = 0;
+            if (edge_ok && used >= 4) {
+                const float inv = 1.0f / static_cast<float>(used);
+                const float cx = mx * inv;
+                const float cy = my * inv;
+                const float cxx = mxx * inv - cx * cx;
+                const float cxy = mxy * inv - cx * cy;
+                const float cyy = myy * inv - cy * cy;
+                const float theta = 0.5f * bdmath::atan2(2.0f * cxy, cxx - cyy);
+                float s, c;
+                bdmath::sincos(theta, &s, &c);
+                lines[edge][0] = cx;
+                lines[edge][1] = cy;
+                lines[edge][2] = -s;
+                lines[edge][3] = c;
+                ok = 1;
+            }
+            have[edge] = ok;
+        }
+    }
+    __syncwarp();
+}
+
+// apply_refined_lines (reference :1021-1076) on lanes 0-3: lane i
+// intersects lines i and i + 1 into corner i + 1; the maximum, the side
+// checks and the signed area are then formed in the reference's order from
+// the four lanes' values.  q (shared) is replaced by the refined quad when
+// it is accepted; returns the largest corner move (0 when rejected).
+__device__ float apply_refined_lines_warp(float (*q)[2], const float (*lines)[4], const int* have,
+                                          int lane) {
+    const int line_count = (have[0] ? 1 : 0) + (have[1] ? 1 : 0) + (have[2] ? 1 : 0) + (have[3] ? 1 : 0);
+    if (line_count < 3) return 0.0f;
+    const int i = lane & 3;
+    const int j = (i + 1) & 3;
+    const float qix = q[i][0], qiy = q[i][1];
+    const float qjx = q[j][0], qjy = q[j][1];
+    const float side = bdmath::hypot(qjx - qix, qjy - qiy);
+    float extent = 0.0f;
+    for (int k = 0; k < 4; ++k) extent = fmaxf(extent, __shfl_sync(kFull, side, k));
+    const float max_shift = fminf(fmaxf(0.15f * extent, 4.0f), 16.0f);
+    float rx = qjx, ry = qjy;  // refined corner j
+    float shift = 0.0f;
+    int shifted = 0;
+    if (have[i] && have[j]) {
+        float x, y;
+        if (intersect_lines(lines[i], lines[j], &x, &y)) {
+            const float dx = x - qjx;
+            const float dy = y - qjy;
+            if (!(dx * dx + dy * dy > max_shift * max_shift)) {
+                rx = x;
+                ry = y;
+                shift = sqrtf(dx * dx + dy * dy);
+                shifted = 1;
+            }
+        }
+    }
+    float moved = 0.0f;
+    for (int k = 0; k < 4; ++k) {
+        const float sk = __shfl_sync(kFull, shift, k);
+        if (__shfl_sync(kFull, shifted, k)) moved = fmaxf(moved, sk);
+    }
+    // Refined corner i is held by lane (i + 3) & 3.
+    const float pix = __shfl_sync(kFull, rx, (i + 3) & 3);
+    const float piy = __shfl_sync(kFull, ry, (i + 3) & 3);
+    const bool short_side = bdmath::hypot(rx - pix, ry - piy) < 3.0f;
+    if (__any_sync(kFull, lane < 4 && short_side)) return 0.0f;
+    const float term = pix * ry - rx * piy;
+    float area2 = 0.0f;
+    for (int k = 0; k < 4; ++k) area2 += __shfl_sync(kFull, term, k);
+    if (area2 <= 0.0f) return 0.0f;
+    __syncwarp();
+    if (lane < 4) {
+        q[j][0] = rx;
+        q[j][1] = ry;
+    }
+    __syncwarp();
+    return moved;
+}
+
+// One warp fits one edge for the CTA path of big candidates (reference
+// fit_edge_line_warp :881-1016).  Sample s (< 16) along the edge is probed
+// by lanes s and s + 16, which take the even and odd probe steps and leave
+// the profile in shared memory; lane s then picks the peak exactly as the
+// reference lane does.  The moments sit in lanes 0..15 (zero above), so the
+// shuffle tree sums them in the reference's order.
 __device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8_t* __restrict__ image,
                                    int width, int height, int64_t stride, int dim, bool first_pass,
                                    int lane, float* s_mags, float line[4]) {
@@ -1198,291 +1400,8 @@ __device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8
     return true;
 }
 
-__device__ float apply_refined_lines(float quad[4][2], const float lines[4][4], const int have[4]) {
-    int line_count = 0;
-    for (int i = 0; i < 4; ++i) line_count += have[i] ? 1 : 0;
-    if (line_count < 3) return 0.0f;
-    float refined[4][2];
-    for (int i = 0; i < 4; ++i) {
-        refined[i][0] = quad[i][0];
-        refined[i][1] = quad[i][1];
-    }
-    float extent = 0.0f;
-    for (int i = 0; i < 4; ++i) {
-        const int j = (i + 1) & 3;
-        extent = fmaxf(extent, bdmath::hypot(quad[j][0] - quad[i][0], quad[j][1] - quad[i][1]));
-    }
-    const float max_shift = fminf(fmaxf(0.15f * extent, 4.0f), 16.0f);
-    float moved = 0.0f;
-    for (int i = 0; i < 4; ++i) {
-        const int j = (i + 1) & 3;
-        if (!have[i] || !have[j]) continue;
-        float x, y;
-        if (!intersect_lines(lines[i], lines[j], &x, &y)) continue;
-        const int corner = j;
-        const float dx = x - quad[corner][0];
-        const float dy = y - quad[corner][1];
-        if (dx * dx + dy * dy > max_shift * max_shift) continue;
-        refined[corner][0] = x;
-        refined[corner][1] = y;
-        moved = fmaxf(moved, sqrtf(dx * dx + dy * dy));
-    }
-    for (int i = 0; i < 4; ++i) {
-        const int j = (i + 1) & 3;
-        if (bdmath::hypot(refined[j][0] - refined[i][0], refined[j][1] - refined[i][1]) < 3.0f) {
-            return 0.0f;
-        }
-    }
-    float area2 = 0.0f;
-    for (int i = 0; i < 4; ++i) {
-        const int j = (i + 1) & 3;
-        area2 += refined[i][0] * refined[j][1] - refined[j][0] * refined[i][1];
-    }
-    if (area2 <= 0.0f) return 0.0f;
-    for (int i = 0; i < 4; ++i) {
-        quad[i][0] = refined[i][0];
-        quad[i][1] = refined[i][1];
-    }
-    return moved;
-}
-
-// Flattened (frame, candidate) work list: CTA c takes items c, c + grid, ...
-// The hull is built once per candidate; with 8 warps, warps 0-3 refine the
-// quad for the frame's first requested family and warps 4-7 for the second,
-// concurrently; with 4 warps the families are refined one after the other.
-template <int kFitWarps>
-__global__ void __launch_bounds__(kFitWarps * 32) k_fit(const BatchDesc* __restrict__ b,
-                                                        const FrameIO* __restrict__ io) {
-    __shared__ uint32_t boundary[2 * kMaxBoundaryRows];
-    __shared__ float probe_dot[kFitWarps][kFitDirections];
-    __shared__ uint32_t probe_point[kFitWarps][kFitDirections];
-    __shared__ uint32_t extreme[kFitDirections];
-    __shared__ uint32_t s_hull[kFitDirections];
-    __shared__ int s_hc;
-    __shared__ float hull_quad[4][2];
-    __shared__ float fit_quad[2][4][2];
-    __shared__ float edge_lines[2][4][4];
-    __shared__ int edge_have[2][4];
-    __shared__ int quad_ok;
-    __shared__ int s_done[2];
-    __shared__ float s_mags[kFitWarps][16 * kMaxProbes];
-    __shared__ int s_prefix[kMaxFrames + 1];
-
-    const int tid = threadIdx.x;
-    const int warp = tid >> 5, lane = tid & 31;
-    if (tid == 0) {
-        int run = 0;
-        for (int f = 0; f < b->frames; ++f) {
-            s_prefix[f] = run;
-            run += static_cast<int>(b->f[f].state->n_candidates);
-        }
-        s_prefix[b->frames] = run;
-    }
-    __syncthreads();
-    const int total = s_prefix[b->frames];
-    const int dir = lane;
-    const int part = warp;
-    float ux, uy;
-    {
-        const float angle =
-            6.28318530718f * static_cast<float>(dir) / static_cast<float>(kFitDirections);
-        bdmath::sincos(angle, &uy, &ux);
-    }
-
-    for (int item = blockIdx.x; item < total; item += gridDim.x) {
-        int fi = 0;
-        while (s_prefix[fi + 1] <= item) ++fi;
-        const FrameDesc& d = b->f[fi];
-        const int ci = item - s_prefix[fi];
-        const int mc = d.max_candidates;
-        const uint8_t* __restrict__ gray = io[fi].gray;
-        const int64_t stride = io[fi].stride;
-        const uint32_t root = d.candidates[ci];
-        const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[root];
-        const int x0 = static_cast<int>(bb.x), y0 = static_cast<int>(bb.y);
-        const int x1 = static_cast<int>(bb.z), y1 = static_cast<int>(bb.w);
-        const int rows = y1 - y0 + 1;
-        const int kept = min(rows, kMaxBoundaryRows);
-        const int points = 2 * kept;
-
-        // Leftmost / rightmost run of the component in each sampled row
-        // (reference collect_row_extremes :676-715).
-        for (int s = tid; s < kept; s += blockDim.x) {
-            const int y = y0 + (kept > 1 ? (s * (rows - 1)) / (kept - 1) : 0);
-            const int n = static_cast<int>(d.row_count[y]);
-            const uint32_t* row_runs = d.runs + static_cast<int64_t>(y) * d.row_cap;
-            int lo = 0, hi = n - 1, first = n;
-            while (lo <= hi) {
-                const int mid = (lo + hi) >> 1;
-                if (static_cast<int>(row_runs[mid] >> 16) >= x0) {
-                    first = mid;
-                    hi = mid - 1;
-                } else {
-                    lo = mid + 1;
-                }
-            }
-            const uint32_t* row_label = d.parent + static_cast<int64_t>(y) * d.row_cap;
-            int left = -1, right = -1;
-            // In order from `first`, stopping at the first run past the
-            // bbox; four runs and labels are loaded ahead of the checks.
-            for (int k = first; k < n; k += 4) {
-                uint32_t rr[4], lab[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int kk = min(k + j, n - 1);
-                    rr[j] = row_runs[kk];
-                    lab[j] = row_label[kk];
-                }
-                bool stop = false;
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    if (stop || k + j >= n) continue;
-                    const int rx0 = static_cast<int>(rr[j] & 0xffffu);
-                    const int rx1 = static_cast<int>(rr[j] >> 16);
-                    if (rx0 > x1) {
-                        stop = true;
-                        continue;
-                    }
-                    if (lab[j] != root) continue;
-                    left = left < 0 ? rx0 : min(left, rx0);
-                    right = right < 0 ? rx1 : max(right, rx1);
-                }
-                if (stop) break;
-            }
-            boundary[2 * s] = left < 0 ? kNone : pack_point(left, y);
-            boundary[2 * s + 1] = right < 0 ? kNone : pack_point(right, y);
-        }
-        __syncthreads();
-
-        // Extreme boundary point per direction; the first point wins ties
-        // (reference :1134-1170, eight parts instead of four: same result).
-        const int chunk = (points + kFitWarps - 1) / kFitWarps;
-        const int begin = part * chunk;
-        const int end = min(points, begin + chunk);
-        float best_dot = -FLT_MAX;
-        uint32_t best_point = kNone;
-        for (int i = begin; i < end; ++i) {
-            const uint32_t p = boundary[i];
-            if (p == kNone) continue;
-            const float dd = static_cast<float>(p & 0xffffu) * ux + static_cast<float>(p >> 16) * uy;
-            if (dd > best_dot) {
-                best_dot = dd;
-                best_point = p;
-            }
-        }
-        probe_dot[part][dir] = best_dot;
-        probe_point[part][dir] = best_point;
-        __syncthreads();
-        if (tid < kFitDirections) {
-            float best = -FLT_MAX;
-            uint32_t point = kNone;
-            for (int p = 0; p < kFitWarps; ++p) {
-                if (probe_dot[p][tid] > best) {
-                    best = probe_dot[p][tid];
-                    point = probe_point[p][tid];
-                }
-            }
-            extreme[tid] = point;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            int hc = 0;
-            for (int i = 0; i < kFitDirections; ++i) {
-                const uint32_t p = extreme[i];
-                if (p == kNone) continue;
-                if (hc > 0 && s_hull[hc - 1] == p) continue;
-                s_hull[hc++] = p;
-            }
-            while (hc > 1 && s_hull[0] == s_hull[hc - 1]) --hc;
-            s_hc = hc;
-        }
-        __syncthreads();
-
-        float* hull_out = d.hull_quads + static_cast<int64_t>(ci) * 8;
-        if (warp == 0) {
-            float quad[4][2] = {};
-            const bool ok = hull_to_quad_warp(s_hull, s_hc, quad, lane);
-            if (lane < 8) {
-                const float v = quad[lane >> 1][lane & 1];
-                hull_quad[lane >> 1][lane & 1] = v;
-                fit_quad[0][lane >> 1][lane & 1] = v;
-                fit_quad[1][lane >> 1][lane & 1] = v;
-                hull_out[lane] = ok ? v : bdmath::quiet_nan();
-            }
-            if (lane == 0) {
-                quad_ok = ok ? 1 : 0;
-                if (ok) atomicAdd(&d.state->counts[3], 1u);
-            }
-        }
-        __syncthreads();
-
-        // Families of this frame: slot 0 = lowest requested family.
-        const uint32_t fams = d.families & 3u;
-        const int nfam = __popc(fams);
-        const int fam_of_slot[2] = {(fams & 1u) ? 0 : 1, 1};
-        if (!quad_ok) {
-            if (tid < 8 * nfam) {
-                const int fam = fam_of_slot[tid >> 3];
-                d.quads[(static_cast<int64_t>(fam) * mc + ci) * 8 + (tid & 7)] = bdmath::quiet_nan();
-            }
-            __syncthreads();
-            continue;
-        }
-        constexpr int kSlotsPerPass = kFitWarps / 4;
-        for (int pass0 = 0; d.refine_edges && pass0 < nfam; pass0 += kSlotsPerPass) {
-            const int slot = pass0 + (warp >> 2);
-            const int edge = warp & 3;
-            const bool mine = slot < nfam;
-            const int dim = family_dim(fam_of_slot[slot < nfam ? slot : 0]);
-            if (tid < 2) s_done[tid] = 0;
-            __syncthreads();
-            for (int iteration = 0; iteration < kFitIterations; ++iteration) {
-                if (mine && !s_done[slot]) {
-                    float line[4];
-                    const bool ok = fit_edge_line_warp(fit_quad[slot], edge, gray, d.width, d.height,
-                                                       stride, dim, iteration == 0, lane, s_mags[warp],
-                                                       line);
-                    if (lane == 0) {
-                        edge_have[slot][edge] = ok ? 1 : 0;
-                        if (ok) {
-                            for (int k = 0; k < 4; ++k) edge_lines[slot][edge][k] = line[k];
-                        }
-                    }
-                }
-                __syncthreads();
-                if (lane == 0 && edge == 0 && mine && !s_done[slot]) {
-                    float quad[4][2];
-                    for (int i = 0; i < 4; ++i) {
-                        quad[i][0] = fit_quad[slot][i][0];
-                        quad[i][1] = fit_quad[slot][i][1];
-                    }
-                    const float moved = apply_refined_lines(quad, edge_lines[slot], edge_have[slot]);
-                    for (int i = 0; i < 4; ++i) {
-                        fit_quad[slot][i][0] = quad[i][0];
-                        fit_quad[slot][i][1] = quad[i][1];
-                    }
-                    // Converged quads skip the second pass (reference :1229-1231).
-                    if (moved < 0.15f) s_done[slot] = 1;
-                }
-                __syncthreads();
-            }
-        }
-        if (tid < 8 * nfam) {
-            const int slot = tid >> 3;
-            const int fam = fam_of_slot[slot];
-            d.quads[(static_cast<int64_t>(fam) * mc + ci) * 8 + (tid & 7)] =
-                fit_quad[slot][(tid & 7) >> 1][tid & 1];
-        }
-        __syncthreads();
-    }
-}
-
-// ===========================================================================
-// 8. Decode (reference homography_from_unit_quad :1249, match_code :1274,
-//    decode_quad :1291, k_decode_quads :1438).  CTA = one (frame, family,
-//    candidate); warp v decodes variant v: rotations 0-3 of the refined quad,
-//    then 0-3 of the hull.
-// ===========================================================================
+// ---- decode of one variant (reference homography_from_unit_quad :1249,
+// match_code :1274, decode_quad :1291) ----
 __device__ __forceinline__ bool homography_from_unit_quad(const float quad[4][2], float h[9]) {
     const float x0 = quad[0][0], y0 = quad[0][1];
     const float x1 = quad[1][0], y1 = quad[1][1];
@@ -1513,126 +1432,271 @@ struct VariantResult {
     float corners[8];
 };
 
-constexpr int kDecodeThreads = 256;
-
-__device__ bool decode_variant_warp(const uint8_t* gray, const FrameDesc& d, int64_t stride,
-                                    int fam, const float* src, int rotation, int lane,
-                                    float* s_raw, float* s_sharp, VariantResult* result) {
+// Decodes the four rotations of one quad at once (reference decode_quad
+// :1291-1436, one call per variant there): lanes 8r..8r+7 take rotation r,
+// lane 8r+u sampling cells u, u+8, ... of the dim x dim grid with the
+// reference's expressions.  Per rotation, the valid flag, min/max, border
+// test and code bits are reduced inside the 8-lane group (all, min, max and
+// OR do not depend on order).  Every lane then scores codewords i = lane,
+// lane+32, ... against all four codes (the first codeword at the minimum
+// distance, as match_code :1274), and each group leader forms the decision
+// margin with the reference's row-major sums.  Returns, in all lanes, the
+// rotation with the highest score (4 - hamming) * 1000 + margin, the first
+// on ties, or -1; lane 0 writes its record to *result.
+__device__ int decode_rotations_warp(const uint8_t* __restrict__ gray, const FrameDesc& d,
+                                     int64_t stride, int fam, const float* src, int lane,
+                                     float (*s_raw)[64], float (*s_sharp)[64], VariantResult* result) {
     const int dim = family_dim(fam);
     const int cells = dim * dim;
+    const int g = lane >> 3;
+    const int u = lane & 7;
+    const uint32_t gmask = 0xffu << (8 * g);
     float corners[4][2];
     for (int k = 0; k < 4; ++k) {
-        const int s = (rotation + k) & 3;
+        const int s = (g + k) & 3;
         corners[k][0] = src[s * 2 + 0];
         corners[k][1] = src[s * 2 + 1];
     }
     float h[9];
-    if (!homography_from_unit_quad(corners, h)) return false;
+    bool alive = homography_from_unit_quad(corners, h);
     bool valid = true;
     float mn = 255.0f, mx = 0.0f;
-    for (int c = lane; c < cells; c += 32) {
-        const int cy = c / dim, cx = c - cy * dim;
-        const float u = (cx + 0.5f) / static_cast<float>(dim);
-        const float v = (cy + 0.5f) / static_cast<float>(dim);
-        const float den = h[6] * u + h[7] * v + 1.0f;
-        if (fabsf(den) < 1e-9f) {
-            valid = false;
-            continue;
+    float* raw = s_raw[g];
+    if (alive) {
+        for (int c = u; c < cells; c += 8) {
+            const int cy = c / dim, cx = c - cy * dim;
+            const float uu = (cx + 0.5f) / static_cast<float>(dim);
+            const float vv = (cy + 0.5f) / static_cast<float>(dim);
+            const float den = h[6] * uu + h[7] * vv + 1.0f;
+            if (fabsf(den) < 1e-9f) {
+                valid = false;
+                continue;
+            }
+            const float x = (h[0] * uu + h[1] * vv + h[2]) / den;
+            const float y = (h[3] * uu + h[4] * vv + h[5]) / den;
+            const float value = sample_bilinear(gray, d.width, d.height, stride, x - 0.0f, y - 0.0f);
+            if (value < 0.0f) valid = false;
+            raw[c] = value;
+            mn = fminf(mn, value);
+            mx = fmaxf(mx, value);
         }
-        const float x = (h[0] * u + h[1] * v + h[2]) / den;
-        const float y = (h[3] * u + h[4] * v + h[5]) / den;
-        const float value = sample_bilinear(gray, d.width, d.height, stride, x - 0.0f, y - 0.0f);
-        if (value < 0.0f) valid = false;
-        s_raw[c] = value;
-        mn = fminf(mn, value);
-        mx = fmaxf(mx, value);
     }
-    if (!__all_sync(kFull, valid)) return false;
-    for (int off = 16; off > 0; off >>= 1) {
+    valid = (__ballot_sync(kFull, valid) & gmask) == gmask;
+    for (int off = 4; off > 0; off >>= 1) {
         mn = fminf(mn, __shfl_xor_sync(kFull, mn, off));
         mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, off));
     }
-    if (mx - mn < 10.0f) return false;
+    alive = alive && valid && !(mx - mn < 10.0f);
     const float thresh = 0.5f * (mn + mx);
     bool border_bad = false;
-    for (int c = lane; c < cells; c += 32) {
-        const int cy = c / dim, cx = c - cy * dim;
-        if (cx == 0 || cy == 0 || cx == dim - 1 || cy == dim - 1) {
-            border_bad = border_bad || s_raw[c] >= thresh;
-        }
-    }
-    if (__any_sync(kFull, border_bad)) return false;
-    __syncwarp();
-    for (int c = lane; c < cells; c += 32) s_raw[c] = s_raw[c] - thresh;  // diff
-    __syncwarp();
-    const int nbits = (dim - 2) * (dim - 2);
-    uint64_t code_part = 0;
-    for (int c = lane; c < cells; c += 32) {
-        const int cy = c / dim, cx = c - cy * dim;
-        float sv = s_raw[c];
-        if (cx >= 1 && cy >= 1 && cx <= dim - 2 && cy <= dim - 2) {
-            const float cc = s_raw[c];
-            const float lap = 4.0f * cc - s_raw[c - dim] - s_raw[c + dim] - s_raw[c - 1] - s_raw[c + 1];
-            sv = cc + d.sharpening * lap;
-            const int k = (cy - 1) * (dim - 2) + (cx - 1);
-            if (sv > 0.0f) code_part |= 1ull << (nbits - 1 - k);
-        }
-        s_sharp[c] = sv;
-    }
-    for (int off = 16; off > 0; off >>= 1) code_part |= __shfl_xor_sync(kFull, code_part, off);
-    const uint64_t code = code_part;
-
-    // First codeword at the minimum distance: min over (distance, index).
-    const uint64_t* codes = fam == 0 ? d_codes36h11 : d_codes16h5;
-    const int code_count = fam == 0 ? BD_CODEWORDS_36H11_COUNT : BD_CODEWORDS_16H5_COUNT;
-    uint32_t key = 0xffffffffu;
-    for (int i = lane; i < code_count; i += 32) {
-        const uint32_t dist = static_cast<uint32_t>(__popcll(codes[i] ^ code));
-        key = min(key, (dist << 16) | static_cast<uint32_t>(i));
-    }
-    key = __reduce_min_sync(kFull, key);
-    const int best_dist = static_cast<int>(key >> 16);
-    if (best_dist > d.max_hamming[fam]) return false;
-    __syncwarp();
-    if (lane != 0) return true;
-    // Decision margin: sums in row-major order of the data cells.
-    float white_sum = 0.0f, black_sum = 0.0f;
-    int white_count = 0, black_count = 0;
-    for (int cy = 1; cy <= dim - 2; ++cy) {
-        for (int cx = 1; cx <= dim - 2; ++cx) {
-            const float dv = s_sharp[cy * dim + cx];
-            if (dv > 0.0f) {
-                white_sum += dv;
-                ++white_count;
-            } else {
-                black_sum -= dv;
-                ++black_count;
+    if (alive) {
+        for (int c = u; c < cells; c += 8) {
+            const int cy = c / dim, cx = c - cy * dim;
+            if (cx == 0 || cy == 0 || cx == dim - 1 || cy == dim - 1) {
+                border_bad = border_bad || raw[c] >= thresh;
             }
         }
     }
-    const float white_avg = white_sum / static_cast<float>(max(white_count, 1));
-    const float black_avg = black_sum / static_cast<float>(max(black_count, 1));
-    const float margin = fminf(white_avg, black_avg);
-    if (margin < d.min_margin) return false;
-    result->id = static_cast<int>(key & 0xffffu);
-    result->hamming = best_dist;
-    result->margin = margin;
-    for (int k = 0; k < 4; ++k) {
-        result->corners[k * 2 + 0] = corners[k][0];
-        result->corners[k * 2 + 1] = corners[k][1];
+    alive = alive && (__ballot_sync(kFull, border_bad) & gmask) == 0;
+    __syncwarp();
+    if (alive) {
+        for (int c = u; c < cells; c += 8) raw[c] = raw[c] - thresh;  // diff
     }
-    return true;
+    __syncwarp();
+    const int nbits = (dim - 2) * (dim - 2);
+    uint64_t code_part = 0;
+    if (alive) {
+        float* sharp = s_sharp[g];
+        for (int c = u; c < cells; c += 8) {
+            const int cy = c / dim, cx = c - cy * dim;
+            float sv = raw[c];
+            if (cx >= 1 && cy >= 1 && cx <= dim - 2 && cy <= dim - 2) {
+                const float cc = raw[c];
+                const float lap = 4.0f * cc - raw[c - dim] - raw[c + dim] - raw[c - 1] - raw[c + 1];
+                sv = cc + d.sharpening * lap;
+                const int k = (cy - 1) * (dim - 2) + (cx - 1);
+                if (sv > 0.0f) code_part |= 1ull << (nbits - 1 - k);
+            }
+            sharp[c] = sv;
+        }
+    }
+    for (int off = 4; off > 0; off >>= 1) code_part |= __shfl_xor_sync(kFull, code_part, off);
+    const uint32_t alive_lanes = __ballot_sync(kFull, alive);
+    if (alive_lanes == 0) return -1;
+
+    // Codeword search for the four codes together.
+    const uint64_t* codes = fam == 0 ? d_codes36h11 : d_codes16h5;
+    const int code_count = fam == 0 ? BD_CODEWORDS_36H11_COUNT : BD_CODEWORDS_16H5_COUNT;
+    uint64_t code[4];
+    uint32_t key[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        code[r] = __shfl_sync(kFull, code_part, 8 * r);
+        key[r] = 0xffffffffu;
+    }
+    for (int i = lane; i < code_count; i += 32) {
+        const uint64_t cw = codes[i];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const uint32_t dist = static_cast<uint32_t>(__popcll(cw ^ code[r]));
+            key[r] = min(key[r], (dist << 16) | static_cast<uint32_t>(i));
+        }
+    }
+    uint32_t my_key = 0xffffffffu;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const uint32_t k = __reduce_min_sync(kFull, key[r]);
+        if (g == r) my_key = k;
+    }
+    const int best_dist = static_cast<int>(my_key >> 16);
+    alive = alive && best_dist <= d.max_hamming[fam];
+    __syncwarp();
+    // Decision margin on the group leader: sums in row-major order of the
+    // data cells.
+    float margin = 0.0f;
+    if (alive && u == 0) {
+        const float* sharp = s_sharp[g];
+        float white_sum = 0.0f, black_sum = 0.0f;
+        int white_count = 0, black_count = 0;
+        for (int cy = 1; cy <= dim - 2; ++cy) {
+            for (int cx = 1; cx <= dim - 2; ++cx) {
+                const float dv = sharp[cy * dim + cx];
+                if (dv > 0.0f) {
+                    white_sum += dv;
+                    ++white_count;
+                } else {
+                    black_sum -= dv;
+                    ++black_count;
+                }
+            }
+        }
+        const float white_avg = white_sum / static_cast<float>(max(white_count, 1));
+        const float black_avg = black_sum / static_cast<float>(max(black_count, 1));
+        margin = fminf(white_avg, black_avg);
+        alive = !(margin < d.min_margin);
+    }
+    // Best rotation, first on ties (reference k_decode_quads :1448-1460).
+    int best = -1;
+    float best_score = -1.0f;
+    float best_margin = 0.0f;
+    uint32_t best_key = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const bool ok = __shfl_sync(kFull, alive ? 1 : 0, 8 * r) != 0;
+        const float m = __shfl_sync(kFull, margin, 8 * r);
+        const uint32_t k = __shfl_sync(kFull, my_key, 8 * r);
+        if (!ok) continue;
+        const float score = static_cast<float>(4 - static_cast<int>(k >> 16)) * 1000.0f + m;
+        if (score > best_score) {
+            best_score = score;
+            best = r;
+            best_margin = m;
+            best_key = k;
+        }
+    }
+    if (best >= 0 && lane == 0) {
+        result->id = static_cast<int>(best_key & 0xffffu);
+        result->hamming = static_cast<int>(best_key >> 16);
+        result->margin = best_margin;
+        for (int k = 0; k < 4; ++k) {
+            const int s = (best + k) & 3;
+            result->corners[k * 2 + 0] = src[s * 2 + 0];
+            result->corners[k * 2 + 1] = src[s * 2 + 1];
+        }
+    }
+    __syncwarp();
+    return best;
 }
 
-__global__ void __launch_bounds__(kDecodeThreads) k_decode(const BatchDesc* __restrict__ b,
-                                                           const FrameIO* __restrict__ io) {
-    __shared__ float s_raw[8][64];
-    __shared__ float s_sharp[8][64];
-    __shared__ VariantResult s_res[8];
-    __shared__ int s_ok[8];
-    __shared__ int s_prefix[kMaxFrames + 1];
+// ===========================================================================
+// 7+8. Quad fit and decode, one warp per candidate (reference k_fit_quads
+//    :1081-1241 with helpers :659-1076, and k_decode_quads :1438 with
+//    homography_from_unit_quad :1249, match_code :1274, decode_quad :1291).
+//    The warp builds the hull and its four-corner quad, then for each
+//    requested family refines the quad's edges and decodes it: rotations
+//    0-3 of the refined quad, and rotations 0-3 of the hull quad only when
+//    none of those decoded (the reference's variant order and score).
+// ===========================================================================
 
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+// Per-warp shared memory of k_fit_decode.
+struct QuadSmem {
+    float mags[32 * kMaxProbes];  // one probe profile per lane
+    uint32_t hull[32];
+    float q[4][2];                // quad being refined
+    float hq[4][2];               // hull quad
+    float lines[4][4];
+    int have[4];
+    float raw[4][64];             // per rotation: samples, then differences
+    float sharp[4][64];
+    VariantResult res;
+};
+
+// Leftmost / rightmost run of component `root` in row y within [x0, x1]
+// (reference collect_row_extremes :676-715): binary search for the first
+// run ending at or after x0, then runs in order until one starts past x1.
+__device__ __forceinline__ void row_extremes(const FrameDesc& d, uint32_t root, int x0, int x1, int y,
+                                             uint32_t* left_point, uint32_t* right_point) {
+    const int n = static_cast<int>(d.row_count[y]);
+    const uint32_t* row_runs = d.runs + static_cast<int64_t>(y) * d.row_cap;
+    const uint32_t* row_label = d.parent + static_cast<int64_t>(y) * d.row_cap;
+    int lo = 0, hi = n - 1, first = n;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        if (static_cast<int>(row_runs[mid] >> 16) >= x0) {
+            first = mid;
+            hi = mid - 1;
+        } else {
+            lo = mid + 1;
+        }
+    }
+    int left = -1, right = -1;
+    for (int k = first; k < n; k += 4) {
+        uint32_t rr[4], lab[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int kk = min(k + j, n - 1);
+            rr[j] = row_runs[kk];
+            lab[j] = row_label[kk];
+        }
+        bool stop = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (stop || k + j >= n) continue;
+            const int rx0 = static_cast<int>(rr[j] & 0xffffu);
+            const int rx1 = static_cast<int>(rr[j] >> 16);
+            if (rx0 > x1) {
+                stop = true;
+                continue;
+            }
+            if (lab[j] != root) continue;
+            left = left < 0 ? rx0 : min(left, rx0);
+            right = right < 0 ? rx1 : max(right, rx1);
+        }
+        if (stop) break;
+    }
+    *left_point = left < 0 ? kNone : pack_point(left, y);
+    *right_point = right < 0 ? kNone : pack_point(right, y);
+}
+
+// Whether a candidate goes to the CTA path: a bounding-box side above
+// split_px (0: never).  Both fit-and-decode kernels use this test.
+__device__ __forceinline__ bool big_candidate(uint4 bb, int split_px) {
+    return split_px > 0 && max(bb.z - bb.x, bb.w - bb.y) + 1 > static_cast<uint32_t>(split_px);
+}
+
+// Flattened work list of (frame, candidate, family) items, the families of
+// a candidate adjacent; warp w of CTA c takes items c * warps + w, then
+// strides by grid * warps.  Each warp builds the candidate's hull itself (the
+// warp of the frame's lowest family also stores it), so the families of a
+// candidate proceed concurrently and warps never wait for one another after
+// the work-list prefix.
+__global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict__ b,
+                                                    const FrameIO* __restrict__ io, int split_px) {
+    extern __shared__ __align__(16) uint32_t s_dyn[];
+    __shared__ int s_prefix[kMaxFrames + 1];
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int warps = blockDim.x >> 5;
     if (tid == 0) {
         int run = 0;
         for (int f = 0; f < b->frames; ++f) {
@@ -1642,58 +1706,378 @@ __global__ void __launch_bounds__(kDecodeThreads) k_decode(const BatchDesc* __re
         s_prefix[b->frames] = run;
     }
     __syncthreads();
+    QuadSmem& sm = reinterpret_cast<QuadSmem*>(s_dyn)[warp];
     const int total = s_prefix[b->frames];
-    for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    // Probe direction of this lane (reference :1134-1170).
+    float ux, uy;
+    {
+        const float angle =
+            6.28318530718f * static_cast<float>(lane) / static_cast<float>(kFitDirections);
+        bdmath::sincos(angle, &uy, &ux);
+    }
+
+    for (int item = blockIdx.x * warps + warp; item < total; item += gridDim.x * warps) {
         int fi = 0;
         while (s_prefix[fi + 1] <= item) ++fi;
         const FrameDesc& d = b->f[fi];
-        const int n = static_cast<int>(d.state->n_candidates);
-        int local = item - s_prefix[fi];
-        int fam = 0;
-        if (!(d.families & 1u)) {
-            fam = 1;
-        } else if (local >= n) {
-            fam = 1;
-            local -= n;
-        }
-        const int ci = local;
+        const uint32_t fams = d.families & 3u;
+        const int nfam = __popc(fams);
+        const int local = item - s_prefix[fi];
+        const int ci = local / nfam;
+        const int slot = local - ci * nfam;
+        const int fam = (slot == 0 && (fams & 1u)) ? 0 : 1;
+        const bool first_family = slot == 0;
         const int mc = d.max_candidates;
-        const float* q = d.quads + (static_cast<int64_t>(fam) * mc + ci) * 8;
-        const float* hq = d.hull_quads + static_cast<int64_t>(ci) * 8;
-        DecodeOut* out = d.decodes + static_cast<int64_t>(fam) * mc + ci;
-        if (q[0] != q[0]) {
-            if (tid == 0) out->id = -1;
-            continue;  // uniform across the CTA
-        }
-        const float* src = warp < 4 ? q : hq;
-        const bool ok = decode_variant_warp(io[fi].gray, d, io[fi].stride, fam, src, warp & 3, lane,
-                                            s_raw[warp], s_sharp[warp], &s_res[warp]);
-        if (lane == 0) s_ok[warp] = ok ? 1 : 0;
-        __syncthreads();
-        if (tid == 0) {
-            int best = -1;
-            float best_score = -1.0f;
-            for (int variant = 0; variant < 2 && best < 0; ++variant) {
-                for (int rotation = 0; rotation < 4; ++rotation) {
-                    const int r = variant * 4 + rotation;
-                    if (!s_ok[r]) continue;
-                    const float score =
-                        static_cast<float>(4 - s_res[r].hamming) * 1000.0f + s_res[r].margin;
-                    if (score > best_score) {
-                        best_score = score;
-                        best = r;
+        const uint8_t* __restrict__ gray = io[fi].gray;
+        const int64_t stride = io[fi].stride;
+        const uint32_t root = d.candidates[ci];
+        const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[root];
+        if (big_candidate(bb, split_px)) continue;  // k_fit_decode_big's
+        const int x0 = static_cast<int>(bb.x), y0 = static_cast<int>(bb.y);
+        const int x1 = static_cast<int>(bb.z), y1 = static_cast<int>(bb.w);
+        const int rows = y1 - y0 + 1;
+        const int kept = min(rows, kMaxBoundaryRows);
+
+        // Boundary points in reference order (row s: left, then right) go
+        // to every lane by shuffles; lane = direction keeps the first point
+        // of largest projection.
+        float best_dot = -FLT_MAX;
+        uint32_t best_point = kNone;
+        for (int s0 = 0; s0 < kept; s0 += 32) {
+            uint32_t lp = kNone, rp = kNone;
+            const int s = s0 + lane;
+            if (s < kept) {
+                const int y = y0 + (kept > 1 ? (s * (rows - 1)) / (kept - 1) : 0);
+                row_extremes(d, root, x0, x1, y, &lp, &rp);
+            }
+            const int count = min(32, kept - s0);
+            for (int k = 0; k < count; ++k) {
+                const uint32_t pl = __shfl_sync(kFull, lp, k);
+                const uint32_t pr = __shfl_sync(kFull, rp, k);
+                if (pl != kNone) {
+                    const float dd =
+                        static_cast<float>(pl & 0xffffu) * ux + static_cast<float>(pl >> 16) * uy;
+                    if (dd > best_dot) {
+                        best_dot = dd;
+                        best_point = pl;
+                    }
+                }
+                if (pr != kNone) {
+                    const float dd =
+                        static_cast<float>(pr & 0xffffu) * ux + static_cast<float>(pr >> 16) * uy;
+                    if (dd > best_dot) {
+                        best_dot = dd;
+                        best_point = pr;
                     }
                 }
             }
+        }
+        // Hull: extremes in direction order without repeats of the previous
+        // kept point, and without a last point equal to the first.  The
+        // previous kept point equals the nearest earlier valid extreme.
+        const bool valid = best_point != kNone;
+        const uint32_t vmask = __ballot_sync(kFull, valid);
+        const uint32_t earlier = vmask & lanemask_lt();
+        const int prev_lane = earlier ? 31 - __clz(earlier) : 0;
+        const uint32_t prev_point = __shfl_sync(kFull, best_point, prev_lane);
+        const bool keep = valid && (earlier == 0 || prev_point != best_point);
+        const uint32_t kmask = __ballot_sync(kFull, keep);
+        if (keep) sm.hull[__popc(kmask & lanemask_lt())] = best_point;
+        __syncwarp();
+        int hc = __popc(kmask);
+        while (hc > 1 && sm.hull[0] == sm.hull[hc - 1]) --hc;
+
+        float quad[4][2] = {};
+        const bool quad_ok = hull_to_quad_warp(sm.hull, hc, quad, lane);
+        {
+            float v = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v = lane == k ? quad[k >> 1][k & 1] : v;
+            if (lane < 8) {
+                sm.hq[lane >> 1][lane & 1] = v;
+                sm.q[lane >> 1][lane & 1] = v;
+                if (first_family) {
+                    d.hull_quads[static_cast<int64_t>(ci) * 8 + lane] = quad_ok ? v : bdmath::quiet_nan();
+                }
+            }
+        }
+        if (lane == 0 && quad_ok && first_family) atomicAdd(&d.state->counts[3], 1u);
+        __syncwarp();
+
+        float* quad_out = d.quads + (static_cast<int64_t>(fam) * mc + ci) * 8;
+        DecodeOut* out = d.decodes + static_cast<int64_t>(fam) * mc + ci;
+        if (!quad_ok) {
+            if (lane < 8) quad_out[lane] = bdmath::quiet_nan();
+            if (lane == 0) out->id = -1;
+            continue;
+        }
+        const int dim = family_dim(fam);
+        for (int iteration = 0; d.refine_edges && iteration < kFitIterations; ++iteration) {
+            fit_edges_warp(sm.q, gray, d.width, d.height, stride, dim, iteration == 0, lane, sm.mags,
+                           sm.lines, sm.have);
+            const float moved = apply_refined_lines_warp(sm.q, sm.lines, sm.have, lane);
+            // Converged quads skip the second pass (reference :1229-1231).
+            if (moved < 0.15f) break;
+        }
+        if (lane < 8) quad_out[lane] = sm.q[lane >> 1][lane & 1];
+
+        // Decode: the refined quad's rotations, then the hull quad's only
+        // when none of those decoded.
+        int best = decode_rotations_warp(gray, d, stride, fam, &sm.q[0][0], lane, sm.raw, sm.sharp,
+                                         &sm.res);
+        if (best < 0) {
+            best = decode_rotations_warp(gray, d, stride, fam, &sm.hq[0][0], lane, sm.raw, sm.sharp,
+                                         &sm.res);
+        }
+        if (lane == 0) {
             if (best < 0) {
                 out->id = -1;
             } else {
-                out->id = s_res[best].id;
-                out->hamming = s_res[best].hamming;
-                out->margin = s_res[best].margin;
-                for (int k = 0; k < 8; ++k) out->corners[k] = s_res[best].corners[k];
+                out->id = sm.res.id;
+                out->hamming = sm.res.hamming;
+                out->margin = sm.res.margin;
+                for (int k = 0; k < 8; ++k) out->corners[k] = sm.res.corners[k];
             }
         }
+        __syncwarp();
+    }
+}
+
+
+// Candidates above the split, one CTA (8 warps) each: the boundary rows are
+// spread over 256 threads, every warp takes a slice of the boundary for the
+// 32 probe directions, warp 0 builds the hull and its quad, warps 4s..4s+3
+// refine the quad of family slot s (one warp per edge, in place of one lane
+// group per edge), and warps 2s / 2s+1 decode the refined / hull quad of
+// slot s (the hull result is used only when no refined rotation decodes).
+// CTA c takes the big candidates of rank c, c + grid, ... in work-list order.
+__global__ void __launch_bounds__(256) k_fit_decode_big(const BatchDesc* __restrict__ b,
+                                                        const FrameIO* __restrict__ io, int split_px) {
+    constexpr int kWarps = 8;
+    __shared__ uint32_t boundary[2 * kMaxBoundaryRows];
+    __shared__ float probe_dot[kWarps][kFitDirections];
+    __shared__ uint32_t probe_point[kWarps][kFitDirections];
+    __shared__ uint32_t s_hull[kFitDirections];
+    __shared__ float hull_quad[4][2];
+    __shared__ float fit_quad[2][4][2];
+    __shared__ float edge_lines[2][4][4];
+    __shared__ int edge_have[2][4];
+    __shared__ int quad_ok;
+    __shared__ int s_done[2];
+    __shared__ float s_mags[kWarps][16 * kMaxProbes];
+    __shared__ float s_raw[4][4][64];
+    __shared__ float s_sharp[4][4][64];
+    __shared__ VariantResult s_res[4];
+    __shared__ int s_best[4];
+    __shared__ int s_prefix[kMaxFrames + 1];
+    __shared__ int s_wcount[kWarps];
+    __shared__ int s_work[256];
+    __shared__ int s_nwork;
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        int run = 0;
+        for (int f = 0; f < b->frames; ++f) {
+            s_prefix[f] = run;
+            run += static_cast<int>(b->f[f].state->n_candidates);
+        }
+        s_prefix[b->frames] = run;
+        s_nwork = 0;
+    }
+    __syncthreads();
+    const int total = s_prefix[b->frames];
+    float ux, uy;
+    {
+        const float angle =
+            6.28318530718f * static_cast<float>(lane) / static_cast<float>(kFitDirections);
+        bdmath::sincos(angle, &uy, &ux);
+    }
+
+    int running = 0;  // big candidates before this chunk
+    for (int base = 0; base < total; base += blockDim.x) {
+        // This CTA's share of the chunk's big candidates.
+        const int cand = base + tid;
+        bool big = false;
+        if (cand < total) {
+            int fi = 0;
+            while (s_prefix[fi + 1] <= cand) ++fi;
+            const FrameDesc& d = b->f[fi];
+            const uint32_t root = d.candidates[cand - s_prefix[fi]];
+            big = big_candidate(reinterpret_cast<const uint4*>(d.bbox)[root], split_px);
+        }
+        const uint32_t wb = __ballot_sync(kFull, big);
+        if (lane == 0) s_wcount[warp] = __popc(wb);
+        __syncthreads();
+        int before = running, chunk = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            if (w < warp) before += s_wcount[w];
+            chunk += s_wcount[w];
+        }
+        if (big) {
+            const int rank = before + __popc(wb & lanemask_lt());
+            if (rank % static_cast<int>(gridDim.x) == static_cast<int>(blockIdx.x)) {
+                s_work[atomicAdd(&s_nwork, 1)] = cand;
+            }
+        }
+        running += chunk;
+        __syncthreads();
+        const int nwork = s_nwork;
+
+        for (int w = 0; w < nwork; ++w) {
+            const int item = s_work[w];
+            int fi = 0;
+            while (s_prefix[fi + 1] <= item) ++fi;
+            const FrameDesc& d = b->f[fi];
+            const int ci = item - s_prefix[fi];
+            const int mc = d.max_candidates;
+            const uint8_t* __restrict__ gray = io[fi].gray;
+            const int64_t stride = io[fi].stride;
+            const uint32_t root = d.candidates[ci];
+            const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[root];
+            const int x0 = static_cast<int>(bb.x), y0 = static_cast<int>(bb.y);
+            const int x1 = static_cast<int>(bb.z), y1 = static_cast<int>(bb.w);
+            const int rows = y1 - y0 + 1;
+            const int kept = min(rows, kMaxBoundaryRows);
+            const int points = 2 * kept;
+
+            for (int s = tid; s < kept; s += blockDim.x) {
+                const int y = y0 + (kept > 1 ? (s * (rows - 1)) / (kept - 1) : 0);
+                row_extremes(d, root, x0, x1, y, &boundary[2 * s], &boundary[2 * s + 1]);
+            }
+            __syncthreads();
+            // Extreme point per direction over this warp's slice; slices
+            // are merged in order, so the first point still wins ties.
+            {
+                const int slice = (points + kWarps - 1) / kWarps;
+                const int begin = warp * slice;
+                const int end = min(points, begin + slice);
+                float best_dot = -FLT_MAX;
+                uint32_t best_point = kNone;
+                for (int i = begin; i < end; ++i) {
+                    const uint32_t p = boundary[i];
+                    if (p == kNone) continue;
+                    const float dd =
+                        static_cast<float>(p & 0xffffu) * ux + static_cast<float>(p >> 16) * uy;
+                    if (dd > best_dot) {
+                        best_dot = dd;
+                        best_point = p;
+                    }
+                }
+                probe_dot[warp][lane] = best_dot;
+                probe_point[warp][lane] = best_point;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                float best_dot = -FLT_MAX;
+                uint32_t best_point = kNone;
+                for (int p = 0; p < kWarps; ++p) {
+                    if (probe_dot[p][lane] > best_dot) {
+                        best_dot = probe_dot[p][lane];
+                        best_point = probe_point[p][lane];
+                    }
+                }
+                const bool valid = best_point != kNone;
+                const uint32_t vmask = __ballot_sync(kFull, valid);
+                const uint32_t earlier = vmask & lanemask_lt();
+                const int prev_lane = earlier ? 31 - __clz(earlier) : 0;
+                const uint32_t prev_point = __shfl_sync(kFull, best_point, prev_lane);
+                const bool keep = valid && (earlier == 0 || prev_point != best_point);
+                const uint32_t kmask = __ballot_sync(kFull, keep);
+                if (keep) s_hull[__popc(kmask & lanemask_lt())] = best_point;
+                __syncwarp();
+                int hc = __popc(kmask);
+                while (hc > 1 && s_hull[0] == s_hull[hc - 1]) --hc;
+                float quad[4][2] = {};
+                const bool ok = hull_to_quad_warp(s_hull, hc, quad, lane);
+                float v = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) v = lane == k ? quad[k >> 1][k & 1] : v;
+                if (lane < 8) {
+                    hull_quad[lane >> 1][lane & 1] = v;
+                    fit_quad[0][lane >> 1][lane & 1] = v;
+                    fit_quad[1][lane >> 1][lane & 1] = v;
+                    d.hull_quads[static_cast<int64_t>(ci) * 8 + lane] = ok ? v : bdmath::quiet_nan();
+                }
+                if (lane == 0) {
+                    quad_ok = ok ? 1 : 0;
+                    if (ok) atomicAdd(&d.state->counts[3], 1u);
+                }
+            }
+            __syncthreads();
+
+            const uint32_t fams = d.families & 3u;
+            const int nfam = __popc(fams);
+            const int fam_of_slot[2] = {(fams & 1u) ? 0 : 1, 1};
+            if (!quad_ok) {
+                if (tid < 8 * nfam) {
+                    const int fam = fam_of_slot[tid >> 3];
+                    d.quads[(static_cast<int64_t>(fam) * mc + ci) * 8 + (tid & 7)] = bdmath::quiet_nan();
+                }
+                if (tid < nfam) d.decodes[static_cast<int64_t>(fam_of_slot[tid]) * mc + ci].id = -1;
+                __syncthreads();
+                continue;
+            }
+            if (d.refine_edges) {
+                const int slot = warp >> 2;
+                const int edge = warp & 3;
+                const bool mine = slot < nfam;
+                const int dim = family_dim(fam_of_slot[mine ? slot : 0]);
+                if (tid < 2) s_done[tid] = 0;
+                __syncthreads();
+                for (int iteration = 0; iteration < kFitIterations; ++iteration) {
+                    if (mine && !s_done[slot]) {
+                        float line[4];
+                        const bool ok = fit_edge_line_warp(fit_quad[slot], edge, gray, d.width, d.height,
+                                                           stride, dim, iteration == 0, lane, s_mags[warp],
+                                                           line);
+                        if (lane == 0) {
+                            edge_have[slot][edge] = ok ? 1 : 0;
+                            if (ok) {
+                                for (int k = 0; k < 4; ++k) edge_lines[slot][edge][k] = line[k];
+                            }
+                        }
+                    }
+                    __syncthreads();
+                    if (edge == 0 && mine && !s_done[slot]) {
+                        const float moved =
+                            apply_refined_lines_warp(fit_quad[slot], edge_lines[slot], edge_have[slot], lane);
+                        // Converged quads skip the second pass (reference :1229-1231).
+                        if (lane == 0 && moved < 0.15f) s_done[slot] = 1;
+                    }
+                    __syncthreads();
+                }
+            }
+            if (tid < 8 * nfam) {
+                const int slot = tid >> 3;
+                const int fam = fam_of_slot[slot];
+                d.quads[(static_cast<int64_t>(fam) * mc + ci) * 8 + (tid & 7)] =
+                    fit_quad[slot][(tid & 7) >> 1][tid & 1];
+            }
+            if (warp < 2 * nfam) {
+                const int slot = warp >> 1;
+                const float* src = (warp & 1) == 0 ? &fit_quad[slot][0][0] : &hull_quad[0][0];
+                const int best = decode_rotations_warp(gray, d, stride, fam_of_slot[slot], src, lane,
+                                                       s_raw[warp], s_sharp[warp], &s_res[warp]);
+                if (lane == 0) s_best[warp] = best;
+            }
+            __syncthreads();
+            if (tid < nfam) {
+                DecodeOut* out = d.decodes + static_cast<int64_t>(fam_of_slot[tid]) * mc + ci;
+                const int pick = s_best[2 * tid] >= 0 ? 2 * tid : (s_best[2 * tid + 1] >= 0 ? 2 * tid + 1 : -1);
+                if (pick < 0) {
+                    out->id = -1;
+                } else {
+                    out->id = s_res[pick].id;
+                    out->hamming = s_res[pick].hamming;
+                    out->margin = s_res[pick].margin;
+                    for (int k = 0; k < 8; ++k) out->corners[k] = s_res[pick].corners[k];
+                }
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+        if (tid == 0) s_nwork = 0;
         __syncthreads();
     }
 }
@@ -1853,29 +2237,35 @@ __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __r
 
 int prepare_pipeline() {
     // Shared memory beyond 48 KB per block needs an opt-in, per device.
-    return cudaFuncSetAttribute(k_binarize_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(kBandSmemBytes)) == cudaSuccess ? 0 : -1;
+    if (cudaFuncSetAttribute(k_binarize_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kBandSmemBytes)) != cudaSuccess) {
+        return -1;
+    }
+    return cudaFuncSetAttribute(k_fit_decode, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(kMaxQuadWarps * sizeof(QuadSmem))) == cudaSuccess
+               ? 0
+               : -1;
 }
 
 const char* const kStageNames[kStageCount] = {
     "stats", "binarize_runs", "merge", "region_stats", "cand_count",
-    "cand_emit", "fit", "decode", "finalize"};
+    "cand_emit", "fit_decode_big", "fit_decode", "finalize"};
 
 void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* io, void* stream_ptr,
-                      const LaunchConfig& lc, int sm_count, void* const* stage_events) {
+                      const LaunchConfig& lc, int sm_count, const ForkJoin* fork,
+                      void* const* stage_events) {
     cudaStream_t s = static_cast<cudaStream_t>(stream_ptr);
     auto mark = [&](int k) {
         if (stage_events) cudaEventRecord(static_cast<cudaEvent_t>(stage_events[k]), s);
     };
     const int bands = hd.total_bands;
-    int cand_total = 0;
-    int dec_total = 0;
+    int items = 0;  // candidate-family pairs at the caps
     for (int f = 0; f < hd.frames; ++f) {
-        cand_total += hd.f[f].max_candidates;
-        dec_total += hd.f[f].max_candidates * __builtin_popcount(hd.f[f].families & 3u);
+        items += hd.f[f].max_candidates * __builtin_popcount(hd.f[f].families & 3u);
     }
-    const int fit_grid = std::max(1, std::min(cand_total, sm_count * lc.fit_ctas_per_sm));
-    const int dec_grid = std::max(1, std::min(dec_total, sm_count * lc.decode_ctas_per_sm));
+    const int warps = lc.quad_warps;
+    const int quad_grid =
+        std::max(1, std::min((items + warps - 1) / warps, sm_count * lc.quad_ctas_per_sm));
     mark(0);
     k_stats<<<hd.stats_ctas, 256, 0, s>>>(dd, io);
     mark(1);
@@ -1889,14 +2279,28 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     mark(5);
     k_cand_emit<<<bands, 256, 0, s>>>(dd, io);
     mark(6);
-    if (lc.fit_warps == 4) {
-        k_fit<4><<<fit_grid, 128, 0, s>>>(dd, io);
+    const int split = lc.quad_split;
+    int cands = 0;
+    for (int f = 0; f < hd.frames; ++f) cands += hd.f[f].max_candidates;
+    const int big_grid = std::max(1, std::min(cands, sm_count));
+    const size_t quad_smem = warps * sizeof(QuadSmem);
+    if (split > 0 && fork && !stage_events) {
+        // Big candidates on a parallel branch (a fork/join in the graph).
+        cudaStream_t s2 = static_cast<cudaStream_t>(fork->stream);
+        cudaEventRecord(static_cast<cudaEvent_t>(fork->fork_event), s);
+        cudaStreamWaitEvent(s2, static_cast<cudaEvent_t>(fork->fork_event), 0);
+        k_fit_decode_big<<<big_grid, 256, 0, s2>>>(dd, io, split);
+        cudaEventRecord(static_cast<cudaEvent_t>(fork->join_event), s2);
+        k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io, split);
+        cudaStreamWaitEvent(s, static_cast<cudaEvent_t>(fork->join_event), 0);
+        mark(7);
+        mark(8);
     } else {
-        k_fit<8><<<fit_grid, 256, 0, s>>>(dd, io);
+        if (split > 0) k_fit_decode_big<<<big_grid, 256, 0, s>>>(dd, io, split);
+        mark(7);
+        k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io, split);
+        mark(8);
     }
-    mark(7);
-    k_decode<<<dec_grid, kDecodeThreads, 0, s>>>(dd, io);
-    mark(8);
     k_finalize<<<hd.frames * 2, kFinalThreads, 0, s>>>(dd);
     mark(9);
 }

@@ -110,11 +110,20 @@ struct BatchDesc {
 };
 
 // Launch shapes that do not change any result (tuned per plan).
+constexpr int kMaxQuadWarps = 8;
 struct LaunchConfig {
     int stats_rows = 1;        // tile rows per k_stats CTA: 1, 2 or 4
-    int fit_warps = 8;         // 8: both families refined concurrently; 4: one after the other
-    int fit_ctas_per_sm = 8;   // persistent fit grid = SMs * this (capped by the work)
-    int decode_ctas_per_sm = 6;
+    int quad_warps = 4;        // warps (= candidates in flight) per k_fit_decode CTA: 2, 4 or 8
+    int quad_ctas_per_sm = 8;  // persistent fit/decode grid = SMs * this (capped by the work)
+    int quad_split = 48;       // candidates with a bbox side above this (px) take a CTA each; 0: none
+};
+
+// A second stream and two events for the parallel branch of the pipeline
+// (the CTA path of big candidates); events without timing.
+struct ForkJoin {
+    void* stream;
+    void* fork_event;
+    void* join_event;
 };
 
 // Fills the stats fields of a host BatchDesc for `rows` tile rows per CTA.
@@ -138,9 +147,11 @@ BDGB_HD inline size_t result_bytes(int max_detections) {
 }
 
 // Launch sequence of one batch on one stream (kernels.cu).  `io` is a
-// device array of FrameIO, one per frame.  When stage_events is not null it
-// holds kStageCount + 1 cudaEvent_t, recorded before the first kernel and
-// after every kernel, so consecutive events bracket one stage.
+// device array of FrameIO, one per frame.  With `fork` the big-candidate
+// kernel runs on fork->stream beside the warp-per-candidate kernel.  When
+// stage_events is not null (no fork then) it holds kStageCount + 1
+// cudaEvent_t, recorded before the first kernel and after every kernel, so
+// consecutive events bracket one stage.
 constexpr int kStageCount = 9;
 // Per-device kernel attributes; call with the device current before the
 // first enqueue.  0 on success.
@@ -148,6 +159,6 @@ int prepare_pipeline();
 extern const char* const kStageNames[kStageCount];
 void enqueue_pipeline(const BatchDesc* device_desc, const BatchDesc& host_desc,
                       const FrameIO* device_io, void* stream, const LaunchConfig& launch,
-                      int sm_count, void* const* stage_events = nullptr);
+                      int sm_count, const ForkJoin* fork, void* const* stage_events = nullptr);
 
 }  // namespace bdgb

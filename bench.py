@@ -154,8 +154,8 @@ def tune_throughput(plans, streams, frame_sets, steps=400, strides=None):
     each candidate timed on the same multi-stream loop the benchmark reports
     (frames/s); keeps the fastest on every plan.  Launch shapes never change
     results."""
-    grid = [("fit_warps", [8, 4]), ("fit_ctas_per_sm", [2, 4, 8, 16]),
-            ("decode_ctas_per_sm", [2, 4, 6, 8]), ("stats_rows", [1, 2, 4])]
+    grid = [("quad_split", [32, 48, 64, 96, 0]), ("quad_warps", [2, 4, 8]),
+            ("quad_ctas_per_sm", [2, 4, 8, 16]), ("stats_rows", [1, 2, 4])]
     best = dict(plans[0].launch())
 
     def score(cfg):

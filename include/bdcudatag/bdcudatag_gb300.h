@@ -80,23 +80,25 @@ BD_API int32_t bd_batch_set_stream(bd_batch* batch, void* cuda_stream);
 
 /* Launch shapes of a batch.  None of them changes any result; they only
  * trade parallelism against per-CTA work:
- *   stats_rows          tile rows per CTA of the tile-statistics kernel: 1, 2, 4
- *   fit_warps           8: the two families' edge refinement runs concurrently
- *                       in one CTA per candidate; 4: one after the other
- *   fit_ctas_per_sm     persistent quad-fit grid, CTAs per SM (1..32)
- *   decode_ctas_per_sm  persistent decode grid, CTAs per SM (1..32) */
+ *   stats_rows        tile rows per CTA of the tile-statistics kernel: 1, 2, 4
+ *   quad_warps        warps per CTA of the fit-and-decode kernel, one
+ *                     (candidate, family) per warp: 2, 4, 8
+ *   quad_ctas_per_sm  persistent fit-and-decode grid, CTAs per SM (1..32)
+ *   quad_split        candidates whose bounding box has a side above this
+ *                     many pixels are fitted and decoded by a whole CTA on a
+ *                     parallel branch instead (0: none; 0..4096) */
 typedef struct bd_launch_config {
     int32_t stats_rows;
-    int32_t fit_warps;
-    int32_t fit_ctas_per_sm;
-    int32_t decode_ctas_per_sm;
+    int32_t quad_warps;
+    int32_t quad_ctas_per_sm;
+    int32_t quad_split;
 } bd_launch_config;
 
 BD_API int32_t bd_batch_get_launch(const bd_batch* batch, bd_launch_config* out);
 /* Sets the launch shapes and re-captures the batch's CUDA graphs. */
 BD_API int32_t bd_batch_set_launch(bd_batch* batch, const bd_launch_config* launch);
 /* Autotuner: times candidate launch shapes on `iterations` runs of the given
- * device frames (coordinate descent over the four fields, median GPU time
+ * device frames (coordinate descent over the four shapes, median GPU time
  * per batch) and keeps the fastest; writes it to best_out and its time to
  * best_ms_out (either may be NULL). */
 BD_API int32_t bd_batch_autotune(bd_batch* batch, const uint8_t* const* frames_device,

@@ -259,19 +259,21 @@ def test_launch_shapes_and_autotune_keep_results():
     strides = [w for w, _ in sizes]
     batch = bdcudatag.Batch([(w, h, 3) for w, h in sizes])
     found, out = batch.detect(dev, strides, device=True)
-    shapes = [dict(stats_rows=2), dict(stats_rows=4, fit_warps=4),
-              dict(fit_ctas_per_sm=2, decode_ctas_per_sm=2),
-              dict(stats_rows=1, fit_warps=8, fit_ctas_per_sm=16, decode_ctas_per_sm=8)]
+    shapes = [dict(stats_rows=2), dict(stats_rows=4, quad_warps=2, quad_split=0),
+              dict(quad_ctas_per_sm=1, quad_warps=2, quad_split=16),
+              dict(stats_rows=1, quad_warps=8, quad_ctas_per_sm=16, quad_split=96)]
     for shape in shapes:
         batch.set_launch(**shape)
         f2, o2 = batch.detect(dev, strides, device=True)
         assert np.array_equal(f2, found) and o2.tobytes() == out.tobytes(), shape
     best, ms = batch.autotune(dev, strides, iterations=4)
-    assert ms > 0 and best["fit_warps"] in (4, 8)
+    assert ms > 0 and best["quad_warps"] in (2, 4, 8)
     f3, o3 = batch.detect(dev, strides, device=True)
     assert np.array_equal(f3, found) and o3.tobytes() == out.tobytes()
     with pytest.raises(RuntimeError):
         batch.set_launch(stats_rows=3)
+    with pytest.raises(RuntimeError):
+        batch.set_launch(quad_warps=3)
     # the single-frame path agrees with the batch
     for i in (0, 5, 10, 15):
         w, h = sizes[i]
