@@ -222,6 +222,13 @@ def measure_roofline(plan, frame_sets, peaks):
         "binarize_runs": W * H + ((W + 31) // 32) * 4 * H,  # frame band read, bit rows written
     }
     stage_bytes = per_frame.get(dom, W * H) * BATCH
+    traffic = {}
+    tf = REPO / "profiles" / "dram_traffic.txt"
+    if tf.exists():
+        for line in tf.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 2 and not line.startswith("#"):
+                traffic[parts[0]] = int(parts[1])
     achieved = stage_bytes / (mean[dom] * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs")
     return {
@@ -229,7 +236,8 @@ def measure_roofline(plan, frame_sets, peaks):
         "unit": "GB/s", "frac": round(achieved / peak, 5) if peak else None,
         "frac_of": "measured copy bandwidth (MEASURED_PEAKS.json)",
         "bytes_per_launch": stage_bytes, "mean_launch_ms": round(mean[dom], 5),
-        "traffic": None,
+        "traffic": traffic.get(f"k_{dom}"),
+        "traffic_source": "ncu dram__bytes_read+write per launch, profiles/dram_traffic.txt",
         "stage_ms": {k: round(v, 5) for k, v in mean.items()},
         "stage_share": {k: round(v / total, 4) for k, v in mean.items()},
     }
@@ -615,7 +623,7 @@ def bench_ours(args, rank, world, local_rank):
     cpu = measure_cpu_baseline(frames)
     serving = measure_serving(args.serving_seconds) if args.serving_seconds > 0 else None
     refine = measure_refine()
-    config3 = measure_config3(max(50, args.steps // 20))
+    config3 = measure_config3(max(200, args.steps // 5), streams=args.streams)
     result_bytes = BATCH * ((32 + 2 * plans[0].max_detections * 84 + 255) // 256 * 256)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
