@@ -84,7 +84,8 @@ class RefineArgs(ctypes.Structure):
 
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("stats_rows", ctypes.c_int32), ("quad_warps", ctypes.c_int32),
-                ("quad_ctas_per_sm", ctypes.c_int32), ("quad_split", ctypes.c_int32)]
+                ("quad_ctas_per_sm", ctypes.c_int32), ("quad_split", ctypes.c_int32),
+                ("band_cap", ctypes.c_int32)]
 
 
 class Camera(ctypes.Structure):

@@ -526,6 +526,7 @@ int32_t bd_batch_get_launch(const bd_batch* batch, bd_launch_config* out) {
     out->quad_warps = lc.quad_warps;
     out->quad_ctas_per_sm = lc.quad_ctas_per_sm;
     out->quad_split = lc.quad_split;
+    out->band_cap = lc.band_cap;
     return BD_OK;
 }
 
@@ -539,6 +540,7 @@ int32_t bd_batch_set_launch(bd_batch* batch, const bd_launch_config* launch) {
     lc.quad_warps = launch->quad_warps;
     lc.quad_ctas_per_sm = launch->quad_ctas_per_sm;
     lc.quad_split = launch->quad_split;
+    lc.band_cap = launch->band_cap;
     const std::lock_guard<std::mutex> lock(batch->plan->mutex());
     std::string error;
     if (batch->plan->set_launch(lc, &error) != 0) {

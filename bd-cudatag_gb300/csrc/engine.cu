@@ -517,7 +517,7 @@ int Plan::set_launch(const LaunchConfig& lc, std::string* error) {
     if (!(lc.stats_rows == 1 || lc.stats_rows == 2 || lc.stats_rows == 4) ||
         !(lc.quad_warps == 2 || lc.quad_warps == 4 || lc.quad_warps == kMaxQuadWarps) ||
         lc.quad_ctas_per_sm < 1 || lc.quad_ctas_per_sm > 32 || lc.quad_split < 0 ||
-        lc.quad_split > 4096) {
+        lc.quad_split > 4096 || lc.band_cap < 256 || lc.band_cap > 2048) {
         if (error) *error = "launch config out of range";
         return -1;
     }
@@ -561,6 +561,7 @@ int Plan::autotune(const uint8_t* const* frames, const int32_t* strides, int ite
     const int quad_warps[] = {2, 4, 8};
     const int quad_ctas[] = {2, 4, 8, 16};
     const int quad_split[] = {32, 48, 64, 96, 0};
+    const int band_cap[] = {2048, 1024, 512};
     auto try_values = [&](auto field, const int* values, int n) -> int {
         for (int i = 0; i < n; ++i) {
             LaunchConfig lc = best;
@@ -579,6 +580,7 @@ int Plan::autotune(const uint8_t* const* frames, const int32_t* strides, int ite
     if (try_values(&LaunchConfig::quad_warps, quad_warps, 3) != 0) return -1;
     if (try_values(&LaunchConfig::quad_ctas_per_sm, quad_ctas, 4) != 0) return -1;
     if (try_values(&LaunchConfig::quad_split, quad_split, 5) != 0) return -1;
+    if (try_values(&LaunchConfig::band_cap, band_cap, 3) != 0) return -1;
     if (set_launch(best, error) != 0) return -1;
     if (best_ms) *best_ms = best_t;
     return 0;

@@ -325,11 +325,18 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
 //    boundaries and k_region_stats folds band roots into global roots.  The
 //    local root is the band's smallest slot of the component, so every root
 //    is still the component's smallest slot id (reference invariant,
-//    gpu_detector.cu:398-421).  A band with more than kLocalCap runs falls
-//    back to one root per run and full merging in k_merge.
+//    gpu_detector.cu:398-421).  A band with more than `cap` runs (a launch
+//    shape, 256..2048) is cut into row segments of at most `cap` runs,
+//    labelled one after another, and k_merge also joins each segment's
+//    first row to the row above; only a single row longer than `cap` sends
+//    the band back to one root per run and full merging in k_merge.
 // ===========================================================================
-constexpr int kLocalCap = 2048;
-constexpr size_t kBandSmemBytes = 6 * kLocalCap * sizeof(uint32_t);
+constexpr int kMaxBandCap = 2048;
+// Dynamic shared memory of k_binarize_runs: six arrays of `cap` run
+// entries, then the band's bit rows (kTile rows of `words` words).
+__host__ __device__ constexpr size_t band_smem_bytes(int cap, int words) {
+    return (6 * static_cast<size_t>(cap) + kTile * static_cast<size_t>(words)) * sizeof(uint32_t);
+}
 
 __device__ __forceinline__ uint32_t s_find(uint32_t* par, uint32_t x) {
     for (;;) {
@@ -357,19 +364,21 @@ __device__ __forceinline__ void s_union(uint32_t* par, uint32_t a, uint32_t b) {
 }
 
 __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restrict__ b,
-                                                       const FrameIO* __restrict__ io) {
+                                                       const FrameIO* __restrict__ io, int cap,
+                                                       int bits_words) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
     uint32_t* sm_run = s_dyn;
-    uint32_t* sm_par = s_dyn + kLocalCap;
-    uint32_t* sm_area = s_dyn + 2 * kLocalCap;
-    uint32_t* sm_minx = s_dyn + 3 * kLocalCap;
-    uint32_t* sm_maxx = s_dyn + 4 * kLocalCap;
-    uint32_t* sm_rows = s_dyn + 5 * kLocalCap;
+    uint32_t* sm_par = s_dyn + cap;
+    uint32_t* sm_area = s_dyn + 2 * cap;
+    uint32_t* sm_minx = s_dyn + 3 * cap;
+    uint32_t* sm_maxx = s_dyn + 4 * cap;
+    uint32_t* sm_rows = s_dyn + 5 * cap;
+    uint32_t* sm_bits = s_dyn + 6 * cap;  // kTile rows of bits_words words
     __shared__ uint8_t s_thresh[BD_MAX_WIDTH / kTile];
-    __shared__ uint32_t s_bits[kTile][BD_MAX_WIDTH / 32];
     __shared__ uint32_t s_rowtot[kTile];
     __shared__ uint32_t s_rowoff[kTile + 1];
     __shared__ uint32_t s_nroots;
+    __shared__ uint32_t s_segmask;
 
     const int tid = threadIdx.x;
     const int fi = frame_of_band(b, blockIdx.x);
@@ -463,13 +472,13 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
                 }
             }
             d.bits[static_cast<int64_t>(y) * words + wx] = m;
-            s_bits[w][wx] = m;
+            sm_bits[w * bits_words + wx] = m;
         }
         __syncwarp();
         // Fragments per lane, then the row's prefix (reference :448-470).
         uint32_t cnt = 0;
         for (int c = c0; c < c1; ++c) {
-            const uint32_t m = s_bits[w][c];
+            const uint32_t m = sm_bits[w * bits_words + c];
             cnt += __popc(~m & ((m << 1) | 1u));
         }
         uint32_t incl = cnt;
@@ -495,10 +504,27 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
         s_rowoff[kTile] = off;
         s_nroots = 0;
         atomicAdd(&st->counts[2], off);
+        // Row segments that fit `cap` runs: a segment starts at row r > 0
+        // (bit r) where adding row r would exceed the cap.  A row longer
+        // than the cap by itself sends the band to the fallback.
+        uint32_t mask = 0, cum = 0;
+        bool fits = true;
+        for (int r = 0; r < kTile; ++r) {
+            const uint32_t n = s_rowtot[r];
+            if (n > static_cast<uint32_t>(cap)) fits = false;
+            if (cum > 0 && cum + n > static_cast<uint32_t>(cap)) {
+                mask |= 1u << r;
+                cum = 0;
+            }
+            cum += n;
+        }
+        s_segmask = fits ? mask : kNone;
     }
     __syncthreads();
     const uint32_t band_total = s_rowoff[kTile];
-    const bool local = band_total <= static_cast<uint32_t>(kLocalCap);
+    const uint32_t segmask = s_segmask;
+    const bool fallback = segmask == kNone;
+    const bool single = segmask == 0u;  // the whole band fits: runs go straight to shared memory
 
     // Emit the runs (reference :472-503).
     if (w < rows) {
@@ -506,7 +532,7 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
         const uint32_t slot_base = static_cast<uint32_t>(y) * row_cap;
         uint32_t index = first_index;
         for (int c = c0; c < c1; ++c) {
-            const uint32_t m = s_bits[w][c];
+            const uint32_t m = sm_bits[w * bits_words + c];
             uint32_t starts = ~m & ((m << 1) | 1u);
             const int last = min(31, W - 1 - (c << 5));
             while (starts) {
@@ -521,12 +547,12 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
                     const uint32_t id = slot_base + index;
                     const uint32_t packed = (static_cast<uint32_t>(x0) & 0xffffu) | (static_cast<uint32_t>(x1) << 16);
                     d.runs[id] = packed;
-                    if (local) {
+                    if (single) {
                         const uint32_t li = s_rowoff[w] + index;
                         sm_run[li] = packed;
                         sm_par[li] = li;
-                    } else {
-                        // Fallback: every run is its own band root.
+                    } else if (fallback) {
+                        // Every run is its own band root.
                         d.parent[id] = id;
                         d.area[id] = static_cast<uint32_t>(x1 - x0 + 1);
                         reinterpret_cast<uint4*>(d.bbox)[id] = make_uint4(x0, y, x1, y);
@@ -537,93 +563,110 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
             }
         }
     }
-    if (!local) {
+    if (fallback) {
         if (tid == 0) {
             d.lroot_count[ty] = band_total;
             d.band_mode[ty] = 1;
         }
         return;
     }
-    for (uint32_t i = tid; i < band_total; i += blockDim.x) {
-        sm_area[i] = 0u;
-        sm_minx[i] = 0xffffffffu;
-        sm_maxx[i] = 0u;
-        sm_rows[i] = 0u;
-    }
     __syncthreads();
 
-    // Band-local unions (the reference's k_merge_runs rules inside the band).
-    if (w < rows) {
-        const uint32_t n = s_rowtot[w];
-        const uint32_t base = s_rowoff[w];
-        const uint32_t prev_n = w > 0 ? s_rowtot[w - 1] : 0u;
-        const uint32_t pbase = w > 0 ? s_rowoff[w - 1] : 0u;
-        for (uint32_t i = lane; i < n; i += 32) {
-            const uint32_t run = sm_run[base + i];
-            const int x0 = static_cast<int>(run & 0xffffu);
-            const int x1 = static_cast<int>(run >> 16);
-            // Row 0 of the frame is never merged, not even its word-split
-            // fragments (reference k_merge_runs :514 returns for y <= 0).
-            if (i > 0 && y0 + w > 0) {
-                const int px1 = static_cast<int>(sm_run[base + i - 1] >> 16);
-                if (px1 + 1 >= x0) s_union(sm_par, base + i, base + i - 1);
+    // Band-local components, one row segment at a time (one segment when the
+    // band fits).  Local index i of a segment = band index seg_off + i.
+    for (int r0 = 0; r0 < kTile;) {
+        int r1 = r0 + 1;
+        while (r1 < kTile && !((segmask >> r1) & 1u)) ++r1;
+        const uint32_t seg_off = s_rowoff[r0];
+        const uint32_t seg_n = s_rowoff[r1] - seg_off;
+        for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
+            if (!single) {
+                int row = 0;
+                while (row + 1 < kTile && s_rowoff[row + 1] <= seg_off + i) ++row;
+                sm_run[i] = d.runs[static_cast<int64_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row])];
+                sm_par[i] = i;
             }
-            if (prev_n == 0) continue;
-            int lo2 = 0, hi2 = static_cast<int>(prev_n) - 1, first = static_cast<int>(prev_n);
-            while (lo2 <= hi2) {
-                const int mid = (lo2 + hi2) >> 1;
-                if (static_cast<int>(sm_run[pbase + mid] >> 16) >= x0 - 1) {
-                    first = mid;
-                    hi2 = mid - 1;
-                } else {
-                    lo2 = mid + 1;
+            sm_area[i] = 0u;
+            sm_minx[i] = 0xffffffffu;
+            sm_maxx[i] = 0u;
+            sm_rows[i] = 0u;
+        }
+        __syncthreads();
+
+        // Unions inside the segment (the reference's k_merge_runs rules).
+        if (w >= r0 && w < r1 && w < rows) {
+            const uint32_t n = s_rowtot[w];
+            const uint32_t base = s_rowoff[w] - seg_off;
+            const uint32_t prev_n = w > r0 ? s_rowtot[w - 1] : 0u;
+            const uint32_t pbase = w > r0 ? s_rowoff[w - 1] - seg_off : 0u;
+            for (uint32_t i = lane; i < n; i += 32) {
+                const uint32_t run = sm_run[base + i];
+                const int x0 = static_cast<int>(run & 0xffffu);
+                const int x1 = static_cast<int>(run >> 16);
+                // Row 0 of the frame is never merged, not even its word-split
+                // fragments (reference k_merge_runs :514 returns for y <= 0).
+                if (i > 0 && y0 + w > 0) {
+                    const int px1 = static_cast<int>(sm_run[base + i - 1] >> 16);
+                    if (px1 + 1 >= x0) s_union(sm_par, base + i, base + i - 1);
+                }
+                if (prev_n == 0) continue;
+                int lo2 = 0, hi2 = static_cast<int>(prev_n) - 1, first = static_cast<int>(prev_n);
+                while (lo2 <= hi2) {
+                    const int mid = (lo2 + hi2) >> 1;
+                    if (static_cast<int>(sm_run[pbase + mid] >> 16) >= x0 - 1) {
+                        first = mid;
+                        hi2 = mid - 1;
+                    } else {
+                        lo2 = mid + 1;
+                    }
+                }
+                for (int k = first; k < static_cast<int>(prev_n); ++k) {
+                    const int px0 = static_cast<int>(sm_run[pbase + k] & 0xffffu);
+                    if (px0 > x1 + 1) break;
+                    s_union(sm_par, base + i, pbase + k);
                 }
             }
-            for (int k = first; k < static_cast<int>(prev_n); ++k) {
-                const int px0 = static_cast<int>(sm_run[pbase + k] & 0xffffu);
-                if (px0 > x1 + 1) break;
-                s_union(sm_par, base + i, pbase + k);
-            }
         }
-    }
-    __syncthreads();
+        __syncthreads();
 
-    // Band-local roots and their area / bbox.
-    for (uint32_t i = tid; i < band_total; i += blockDim.x) {
-        uint32_t r = i;
-        while (sm_par[r] != r) r = sm_par[r];
-        int row = 0;
-        while (row + 1 < kTile && s_rowoff[row + 1] <= i) ++row;
-        const uint32_t run = sm_run[i];
-        const uint32_t x0 = run & 0xffffu, x1 = run >> 16;
-        atomicAdd(&sm_area[r], x1 - x0 + 1);
-        atomicMin(&sm_minx[r], x0);
-        atomicMax(&sm_maxx[r], x1);
-        atomicOr(&sm_rows[r], 1u << row);
-        // parent link = the local root's slot
-        int rrow = 0;
-        while (rrow + 1 < kTile && s_rowoff[rrow + 1] <= r) ++rrow;
-        const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (i - s_rowoff[row]);
-        const uint32_t rslot = static_cast<uint32_t>(y0 + rrow) * row_cap + (r - s_rowoff[rrow]);
-        d.parent[slot] = rslot;
+        // Segment roots (its smallest slot) and their area / bbox.
+        for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
+            uint32_t r = i;
+            while (sm_par[r] != r) r = sm_par[r];
+            int row = 0;
+            while (row + 1 < kTile && s_rowoff[row + 1] <= seg_off + i) ++row;
+            const uint32_t run = sm_run[i];
+            const uint32_t x0 = run & 0xffffu, x1 = run >> 16;
+            atomicAdd(&sm_area[r], x1 - x0 + 1);
+            atomicMin(&sm_minx[r], x0);
+            atomicMax(&sm_maxx[r], x1);
+            atomicOr(&sm_rows[r], 1u << row);
+            // parent link = the local root's slot
+            int rrow = 0;
+            while (rrow + 1 < kTile && s_rowoff[rrow + 1] <= seg_off + r) ++rrow;
+            const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row]);
+            const uint32_t rslot = static_cast<uint32_t>(y0 + rrow) * row_cap + (seg_off + r - s_rowoff[rrow]);
+            d.parent[slot] = rslot;
+        }
+        __syncthreads();
+        for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
+            if (sm_par[i] != i) continue;
+            int row = 0;
+            while (row + 1 < kTile && s_rowoff[row + 1] <= seg_off + i) ++row;
+            const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row]);
+            const uint32_t rm = sm_rows[i];
+            d.area[slot] = sm_area[i];
+            reinterpret_cast<uint4*>(d.bbox)[slot] =
+                make_uint4(sm_minx[i], static_cast<uint32_t>(y0 + __ffs(rm) - 1), sm_maxx[i],
+                           static_cast<uint32_t>(y0 + 31 - __clz(rm)));
+            d.lroots[band_base + atomicAdd(&s_nroots, 1u)] = slot;
+        }
+        __syncthreads();
+        r0 = r1;
     }
-    __syncthreads();
-    for (uint32_t i = tid; i < band_total; i += blockDim.x) {
-        if (sm_par[i] != i) continue;
-        int row = 0;
-        while (row + 1 < kTile && s_rowoff[row + 1] <= i) ++row;
-        const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (i - s_rowoff[row]);
-        const uint32_t rm = sm_rows[i];
-        d.area[slot] = sm_area[i];
-        reinterpret_cast<uint4*>(d.bbox)[slot] =
-            make_uint4(sm_minx[i], static_cast<uint32_t>(y0 + __ffs(rm) - 1), sm_maxx[i],
-                       static_cast<uint32_t>(y0 + 31 - __clz(rm)));
-        d.lroots[band_base + atomicAdd(&s_nroots, 1u)] = slot;
-    }
-    __syncthreads();
     if (tid == 0) {
         d.lroot_count[ty] = s_nroots;
-        d.band_mode[ty] = 0;
+        d.band_mode[ty] = segmask;  // bit r: row r starts a segment (k_merge joins it to row r - 1)
     }
 }
 
@@ -669,18 +712,23 @@ __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b,
     const int ty = blockIdx.x - b->band_prefix[fi];
     const int row_cap = d.row_cap;
     uint32_t* parent = d.parent;
-    if (d.band_mode[ty] == 0) {
-        // Band-local unions are done: only the first row meets the band
-        // above; its runs are spread over the whole CTA.
-        const int y = ty * kTile;
-        if (y <= 0) return;
-        const int n = static_cast<int>(d.row_count[y]);
-        const int prev_n = static_cast<int>(d.row_count[y - 1]);
-        const uint32_t* cur = d.runs + static_cast<int64_t>(y) * row_cap;
-        const uint32_t* prev = d.runs + static_cast<int64_t>(y - 1) * row_cap;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            merge_run_with_row_above(parent, cur, prev, i, prev_n, static_cast<uint32_t>(y * row_cap),
-                                     static_cast<uint32_t>((y - 1) * row_cap), false);
+    const uint32_t mode = d.band_mode[ty];
+    if (!(mode & 1u)) {
+        // Band-local unions are done: the first row of the band, and the
+        // first row of every further segment (bit r of the mode), meet the
+        // row above; their runs are spread over the whole CTA.
+        for (uint32_t starts = mode | 1u; starts; starts &= starts - 1u) {
+            const int y = ty * kTile + __ffs(starts) - 1;
+            if (y <= 0 || y >= d.height) continue;
+            const int n = static_cast<int>(d.row_count[y]);
+            const int prev_n = static_cast<int>(d.row_count[y - 1]);
+            const uint32_t* cur = d.runs + static_cast<int64_t>(y) * row_cap;
+            const uint32_t* prev = d.runs + static_cast<int64_t>(y - 1) * row_cap;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                merge_run_with_row_above(parent, cur, prev, i, prev_n,
+                                         static_cast<uint32_t>(y * row_cap),
+                                         static_cast<uint32_t>((y - 1) * row_cap), false);
+            }
         }
         return;
     }
@@ -2238,7 +2286,8 @@ __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __r
 int prepare_pipeline() {
     // Shared memory beyond 48 KB per block needs an opt-in, per device.
     if (cudaFuncSetAttribute(k_binarize_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(kBandSmemBytes)) != cudaSuccess) {
+                             static_cast<int>(band_smem_bytes(kMaxBandCap, BD_MAX_WIDTH / 32))) !=
+        cudaSuccess) {
         return -1;
     }
     return cudaFuncSetAttribute(k_fit_decode, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2269,7 +2318,10 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     mark(0);
     k_stats<<<hd.stats_ctas, 256, 0, s>>>(dd, io);
     mark(1);
-    k_binarize_runs<<<bands, 256, kBandSmemBytes, s>>>(dd, io);
+    int words_max = 1;
+    for (int f = 0; f < hd.frames; ++f) words_max = std::max(words_max, hd.f[f].words);
+    k_binarize_runs<<<bands, 256, band_smem_bytes(lc.band_cap, words_max), s>>>(dd, io, lc.band_cap,
+                                                                                 words_max);
     mark(2);
     k_merge<<<bands, 256, 0, s>>>(dd, io);
     mark(3);

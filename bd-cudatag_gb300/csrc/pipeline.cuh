@@ -89,7 +89,8 @@ struct FrameDesc {
     uint32_t* cand_meta;           // slots: bin << 24 | rank in band, or kNone
     uint32_t* lroots;              // slots: per band (at its first slot) the band-local roots
     uint32_t* lroot_count;         // tile_h: band-local roots per band
-    uint32_t* band_mode;           // tile_h: 0 band-local unions done, 1 fallback (one root per run)
+    uint32_t* band_mode;           // tile_h: bit 0 fallback (one root per run), else bit r: row r
+                                   // starts a shared-memory segment (band-local unions done)
     uint32_t* band_bins;           // tile_h * 64 candidate counts, then exclusive prefixes
     uint32_t* candidates;          // max_candidates root slots, canonical order
     FrameState* state;
@@ -116,6 +117,7 @@ struct LaunchConfig {
     int quad_warps = 4;        // warps (= candidates in flight) per k_fit_decode CTA: 2, 4 or 8
     int quad_ctas_per_sm = 8;  // persistent fit/decode grid = SMs * this (capped by the work)
     int quad_split = 48;       // candidates with a bbox side above this (px) take a CTA each; 0: none
+    int band_cap = 2048;       // runs of a band unioned in shared memory (256..2048); more: fallback
 };
 
 // A second stream and two events for the parallel branch of the pipeline

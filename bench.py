@@ -154,8 +154,8 @@ def tune_throughput(plans, streams, frame_sets, steps=400, strides=None):
     each candidate timed on the same multi-stream loop the benchmark reports
     (frames/s); keeps the fastest on every plan.  Launch shapes never change
     results."""
-    grid = [("quad_split", [32, 48, 64, 96, 0]), ("quad_warps", [2, 4, 8]),
-            ("quad_ctas_per_sm", [2, 4, 8, 16]), ("stats_rows", [1, 2, 4])]
+    grid = [("band_cap", [2048, 1024, 512]), ("quad_split", [32, 48, 64, 96, 0]),
+            ("quad_warps", [2, 4, 8]), ("quad_ctas_per_sm", [2, 4, 8, 16]), ("stats_rows", [1, 2, 4])]
     best = dict(plans[0].launch())
 
     def score(cfg):
@@ -583,7 +583,12 @@ def bench_ours(args, rank, world, local_rank):
     if world > 1:
         torch.distributed.barrier()
     tuned, tune_trials = None, None
-    if args.tune or not args.quick:
+    if args.launch:
+        fixed = {k: int(v) for k, v in (kv.split("=") for kv in args.launch.split(","))}
+        for p in plans:
+            p.set_launch(**fixed)
+        tuned = plans[0].launch()
+    elif args.tune or not args.quick:
         # Launch shapes scored on frames/s with all streams busy (untimed).
         tuned, tune_trials = tune_throughput(plans, streams, sets_dev)
     if args.quick:
@@ -666,6 +671,8 @@ def main():
     ap.add_argument("--serving-seconds", type=float, default=60.0,
                     help="length of the config-5 serving run (0: skip)")
     ap.add_argument("--tune", action="store_true", help="tune launch shapes in --quick runs")
+    ap.add_argument("--launch", default="",
+                    help="fixed launch shapes instead of tuning, e.g. band_cap=1024,quad_split=48")
     ap.add_argument("--quick", action="store_true",
                     help="profiling run: 64-frame pool, batched device-input loop only")
     args = ap.parse_args()

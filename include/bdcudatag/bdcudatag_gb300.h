@@ -86,19 +86,22 @@ BD_API int32_t bd_batch_set_stream(bd_batch* batch, void* cuda_stream);
  *   quad_ctas_per_sm  persistent fit-and-decode grid, CTAs per SM (1..32)
  *   quad_split        candidates whose bounding box has a side above this
  *                     many pixels are fitted and decoded by a whole CTA on a
- *                     parallel branch instead (0: none; 0..4096) */
+ *                     parallel branch instead (0: none; 0..4096)
+ *   band_cap          runs of an 8-row band labelled in shared memory
+ *                     (256..2048); a band with more takes the global path */
 typedef struct bd_launch_config {
     int32_t stats_rows;
     int32_t quad_warps;
     int32_t quad_ctas_per_sm;
     int32_t quad_split;
+    int32_t band_cap;
 } bd_launch_config;
 
 BD_API int32_t bd_batch_get_launch(const bd_batch* batch, bd_launch_config* out);
 /* Sets the launch shapes and re-captures the batch's CUDA graphs. */
 BD_API int32_t bd_batch_set_launch(bd_batch* batch, const bd_launch_config* launch);
 /* Autotuner: times candidate launch shapes on `iterations` runs of the given
- * device frames (coordinate descent over the four shapes, median GPU time
+ * device frames (coordinate descent over the five shapes, median GPU time
  * per batch) and keeps the fastest; writes it to best_out and its time to
  * best_ms_out (either may be NULL). */
 BD_API int32_t bd_batch_autotune(bd_batch* batch, const uint8_t* const* frames_device,
@@ -291,6 +294,7 @@ BD_API int32_t bd_tile_stats_device_noalloc(const uint8_t* gray_device, int32_t 
 static_assert(sizeof(bd_camera) == 16, "bd_camera layout changed");
 static_assert(sizeof(bd_server_stats) == 56, "bd_server_stats layout changed");
 static_assert(sizeof(bd_refine_args) == 72, "bd_refine_args layout changed");
+static_assert(sizeof(bd_launch_config) == 20, "bd_launch_config layout changed");
 #endif
 
 #endif /* BDCUDATAG_BDCUDATAG_GB300_H */

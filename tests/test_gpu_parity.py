@@ -259,9 +259,9 @@ def test_launch_shapes_and_autotune_keep_results():
     strides = [w for w, _ in sizes]
     batch = bdcudatag.Batch([(w, h, 3) for w, h in sizes])
     found, out = batch.detect(dev, strides, device=True)
-    shapes = [dict(stats_rows=2), dict(stats_rows=4, quad_warps=2, quad_split=0),
-              dict(quad_ctas_per_sm=1, quad_warps=2, quad_split=16),
-              dict(stats_rows=1, quad_warps=8, quad_ctas_per_sm=16, quad_split=96)]
+    shapes = [dict(stats_rows=2, band_cap=256), dict(stats_rows=4, quad_warps=2, quad_split=0),
+              dict(quad_ctas_per_sm=1, quad_warps=2, quad_split=16, band_cap=512),
+              dict(stats_rows=1, quad_warps=8, quad_ctas_per_sm=16, quad_split=96, band_cap=2048)]
     for shape in shapes:
         batch.set_launch(**shape)
         f2, o2 = batch.detect(dev, strides, device=True)
