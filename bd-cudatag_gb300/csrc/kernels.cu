@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     __shared__ uint32_t s_rowoff[kTile + 1];
     __shared__ uint32_t s_wbin[8][64];
     __shared__ uint32_t s_run[64];
-    __shared__ uint32_t s_chunk[32][64];
+    __shared__ uint32_t s_chunk[4][64];
     __shared__ uint32_t s_total[64];
     __shared__ int s_last;
 
@@ -877,30 +877,28 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     if (!s_last) return;
     __threadfence();
 
-    // Last band: exclusive prefix of every bin over the bands (in place),
-    // 32 bands at a time through shared memory.
+    // Last band: exclusive prefix of every bin over the bands (in place).
+    // Thread (segment q, bin) sums a quarter of the bands (loads coalesced
+    // over the bins), the four segment sums are scanned per bin, and each
+    // thread rewrites its quarter from its segment's offset.
     const int th = d.tile_h;
-    uint32_t carry = 0;  // per bin, owned by thread tid < 64
-    for (int band0 = 0; band0 < th; band0 += 32) {
-        const int nb = min(32, th - band0);
-        for (int k = tid; k < nb * 64; k += blockDim.x) {
-            s_chunk[k >> 6][k & 63] = __ldcg(&d.band_bins[(band0 + (k >> 6)) * 64 + (k & 63)]);
-        }
-        __syncthreads();
-        if (tid < 64) {
-            for (int r = 0; r < nb; ++r) {
-                const uint32_t v = s_chunk[r][tid];
-                s_chunk[r][tid] = carry;
-                carry += v;
-            }
-        }
-        __syncthreads();
-        for (int k = tid; k < nb * 64; k += blockDim.x) {
-            d.band_bins[(band0 + (k >> 6)) * 64 + (k & 63)] = s_chunk[k >> 6][k & 63];
-        }
-        __syncthreads();
+    const int bin = tid & 63;
+    const int q = tid >> 6;
+    const int per = (th + 3) >> 2;
+    const int qb0 = min(th, q * per), qb1 = min(th, qb0 + per);
+    uint32_t sum = 0;
+#pragma unroll 4
+    for (int band = qb0; band < qb1; ++band) sum += __ldcg(&d.band_bins[band * 64 + bin]);
+    s_chunk[q][bin] = sum;
+    __syncthreads();
+    uint32_t carry = 0;
+    for (int q2 = 0; q2 < q; ++q2) carry += s_chunk[q2][bin];
+    if (q == 3) s_total[bin] = carry + sum;
+    for (int band = qb0; band < qb1; ++band) {
+        const uint32_t v = __ldcg(&d.band_bins[band * 64 + bin]);
+        d.band_bins[band * 64 + bin] = carry;
+        carry += v;
     }
-    if (tid < 64) s_total[tid] = carry;
     __syncthreads();
     if (tid == 0) {
         uint32_t pos = 0;
@@ -1483,7 +1481,8 @@ struct VariantResult {
 // Decodes the four rotations of one quad at once (reference decode_quad
 // :1291-1436, one call per variant there): lanes 8r..8r+7 take rotation r,
 // lane 8r+u sampling cells u, u+8, ... of the dim x dim grid with the
-// reference's expressions.  Per rotation, the valid flag, min/max, border
+// reference's expressions (cell centres (c + 0.5f) / dim from cell_uv, the
+// same divisions done once per CTA).  Per rotation, the valid flag, min/max, border
 // test and code bits are reduced inside the 8-lane group (all, min, max and
 // OR do not depend on order).  Every lane then scores codewords i = lane,
 // lane+32, ... against all four codes (the first codeword at the minimum
@@ -1493,7 +1492,8 @@ struct VariantResult {
 // on ties, or -1; lane 0 writes its record to *result.
 __device__ int decode_rotations_warp(const uint8_t* __restrict__ gray, const FrameDesc& d,
                                      int64_t stride, int fam, const float* src, int lane,
-                                     float (*s_raw)[64], float (*s_sharp)[64], VariantResult* result) {
+                                     const float* cell_uv, float (*s_raw)[64], float (*s_sharp)[64],
+                                     VariantResult* result) {
     const int dim = family_dim(fam);
     const int cells = dim * dim;
     const int g = lane >> 3;
@@ -1513,8 +1513,8 @@ __device__ int decode_rotations_warp(const uint8_t* __restrict__ gray, const Fra
     if (alive) {
         for (int c = u; c < cells; c += 8) {
             const int cy = c / dim, cx = c - cy * dim;
-            const float uu = (cx + 0.5f) / static_cast<float>(dim);
-            const float vv = (cy + 0.5f) / static_cast<float>(dim);
+            const float uu = cell_uv[cx];  // (cx + 0.5f) / dim
+            const float vv = cell_uv[cy];
             const float den = h[6] * uu + h[7] * vv + 1.0f;
             if (fabsf(den) < 1e-9f) {
                 valid = false;
@@ -1687,14 +1687,31 @@ __device__ __forceinline__ void row_extremes(const FrameDesc& d, uint32_t root, 
     const int n = static_cast<int>(d.row_count[y]);
     const uint32_t* row_runs = d.runs + static_cast<int64_t>(y) * d.row_cap;
     const uint32_t* row_label = d.parent + static_cast<int64_t>(y) * d.row_cap;
-    int lo = 0, hi = n - 1, first = n;
-    while (lo <= hi) {
-        const int mid = (lo + hi) >> 1;
-        if (static_cast<int>(row_runs[mid] >> 16) >= x0) {
-            first = mid;
-            hi = mid - 1;
-        } else {
-            lo = mid + 1;
+    // First run ending at or after x0 (runs of a row are sorted): eight-way
+    // steps of seven independent loads, then the last <= 8 runs at once.
+    int lo = 0, hi = n;  // the answer lies in [lo, hi]; hi = n: none
+    while (hi - lo > 8) {
+        const int span = hi - lo;
+        uint32_t v[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) v[k] = row_runs[lo + (span * (k + 1)) / 8];
+        int nlo = lo, nhi = hi;
+#pragma unroll
+        for (int k = 6; k >= 0; --k) {
+            const int idx = lo + (span * (k + 1)) / 8;
+            if (static_cast<int>(v[k] >> 16) >= x0) nhi = idx; else if (nlo == lo) nlo = idx + 1;
+        }
+        lo = nlo;
+        hi = nhi;
+    }
+    int first = hi;
+    {
+        uint32_t v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = row_runs[min(lo + k, max(n - 1, 0))];
+#pragma unroll
+        for (int k = 7; k >= 0; --k) {
+            if (lo + k < hi && static_cast<int>(v[k] >> 16) >= x0) first = lo + k;
         }
     }
     int left = -1, right = -1;
@@ -1742,9 +1759,14 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
                                                     const FrameIO* __restrict__ io, int split_px) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
     __shared__ int s_prefix[kMaxFrames + 1];
+    __shared__ float s_uv[2][8];
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int warps = blockDim.x >> 5;
+    if (tid < 16) {
+        const int fam = tid >> 3, c = tid & 7;
+        s_uv[fam][c] = (c + 0.5f) / static_cast<float>(family_dim(fam));
+    }
     if (tid == 0) {
         int run = 0;
         for (int f = 0; f < b->frames; ++f) {
@@ -1871,11 +1893,11 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
 
         // Decode: the refined quad's rotations, then the hull quad's only
         // when none of those decoded.
-        int best = decode_rotations_warp(gray, d, stride, fam, &sm.q[0][0], lane, sm.raw, sm.sharp,
-                                         &sm.res);
+        int best = decode_rotations_warp(gray, d, stride, fam, &sm.q[0][0], lane, s_uv[fam], sm.raw,
+                                         sm.sharp, &sm.res);
         if (best < 0) {
-            best = decode_rotations_warp(gray, d, stride, fam, &sm.hq[0][0], lane, sm.raw, sm.sharp,
-                                         &sm.res);
+            best = decode_rotations_warp(gray, d, stride, fam, &sm.hq[0][0], lane, s_uv[fam], sm.raw,
+                                         sm.sharp, &sm.res);
         }
         if (lane == 0) {
             if (best < 0) {
@@ -1921,9 +1943,14 @@ __global__ void __launch_bounds__(256) k_fit_decode_big(const BatchDesc* __restr
     __shared__ int s_wcount[kWarps];
     __shared__ int s_work[256];
     __shared__ int s_nwork;
+    __shared__ float s_uv[2][8];
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
+    if (tid < 16) {
+        const int fam = tid >> 3, c = tid & 7;
+        s_uv[fam][c] = (c + 0.5f) / static_cast<float>(family_dim(fam));
+    }
     if (tid == 0) {
         int run = 0;
         for (int f = 0; f < b->frames; ++f) {
@@ -2106,7 +2133,8 @@ __global__ void __launch_bounds__(256) k_fit_decode_big(const BatchDesc* __restr
                 const int slot = warp >> 1;
                 const float* src = (warp & 1) == 0 ? &fit_quad[slot][0][0] : &hull_quad[0][0];
                 const int best = decode_rotations_warp(gray, d, stride, fam_of_slot[slot], src, lane,
-                                                       s_raw[warp], s_sharp[warp], &s_res[warp]);
+                                                       s_uv[fam_of_slot[slot]], s_raw[warp],
+                                                       s_sharp[warp], &s_res[warp]);
                 if (lane == 0) s_best[warp] = best;
             }
             __syncthreads();
