@@ -185,6 +185,41 @@ def test_odd_sizes(w, h):
     check_frame(np.ascontiguousarray(img[::-1]), 1)
 
 
+def test_dense_bands_4k():
+    # 3840x2160 serving frames hold 8-row bands of up to ~5000 runs: more
+    # than one shared-memory segment (default cap 2048), so those bands are
+    # labelled in row segments joined by k_merge.
+    img, _ = scenes.render_config(5, 0, 3840, 2160)
+    h, w = img.shape
+    rc = oracle.Frame(img, 0).stage("row_count").astype(np.int64)
+    pad = np.zeros(((h + 7) // 8) * 8, np.int64)
+    pad[:h] = rc[:h]
+    assert pad.reshape(-1, 8).sum(1).max() > 2048  # the segmented path is exercised
+    for fam in (0, 1):
+        check_frame(img, fam, stages=(fam == 0))
+
+
+def test_single_row_over_cap_fallback():
+    # Pixel noise at 8192 px width: rows of ~2000+ runs.  With band_cap 512
+    # one row alone exceeds the cap, so the band takes the one-root-per-run
+    # fallback; results equal the default shapes and the oracle.
+    rng = np.random.default_rng(77)
+    img = rng.integers(0, 256, size=(96, 8192), dtype=np.uint8)
+    img[20:70, 1000:1060] = 30  # a dark block so some components are large
+    n0, ref = check_frame(img, 0)
+    torch = pytest.importorskip("torch")
+    batch = bdcudatag.Batch([(8192, 96, 1)])
+    batch.set_launch(band_cap=512)
+    found, out = batch.detect([torch.from_numpy(img).cuda()], [8192], device=True)
+    assert found[0, 0] == n0 and out[0, 0, :n0].tobytes() == ref.tobytes()
+    lab_fb = batch.stage(0, "label")
+    batch.set_launch(band_cap=2048)
+    batch.detect([torch.from_numpy(img).cuda()], [8192], device=True)
+    rc = batch.stage(0, "row_count")
+    valid = (np.arange(8192 // 2 + 2)[None, :] < rc[:, None]).ravel()
+    assert np.array_equal(lab_fb[valid], batch.stage(0, "label")[valid])
+
+
 def test_caps_exceeded():
     # Clutter frame (index 5) pushes candidates past a small cap; a tiny
     # detection cap truncates in candidate order.
