@@ -1749,6 +1749,10 @@ __device__ __forceinline__ bool big_candidate(uint4 bb, int split_px) {
     return split_px > 0 && max(bb.z - bb.x, bb.w - bb.y) + 1 > static_cast<uint32_t>(split_px);
 }
 
+__device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uint8_t* __restrict__ gray,
+                                  int64_t stride, bool quad_ok, int lane, const float* cell_uv,
+                                  QuadSmem& sm);
+
 // Flattened work list of (frame, candidate, family) items, the families of
 // a candidate adjacent; warp w of CTA c takes items c * warps + w, then
 // strides by grid * warps.  Each warp builds the candidate's hull itself (the
@@ -1797,7 +1801,6 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
         const int slot = local - ci * nfam;
         const int fam = (slot == 0 && (fams & 1u)) ? 0 : 1;
         const bool first_family = slot == 0;
-        const int mc = d.max_candidates;
         const uint8_t* __restrict__ gray = io[fi].gray;
         const int64_t stride = io[fi].stride;
         const uint32_t root = d.candidates[ci];
@@ -1873,13 +1876,24 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
         }
         if (lane == 0 && quad_ok && first_family) atomicAdd(&d.state->counts[3], 1u);
         __syncwarp();
+        fit_decode_family(d, fam, ci, gray, stride, quad_ok, lane, s_uv[fam], sm);
+    }
+}
 
+// Refinement and decode of one (candidate, family) item by one warp, from
+// the hull quad in sm.hq / sm.q.
+__device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uint8_t* __restrict__ gray,
+                                  int64_t stride, bool quad_ok, int lane, const float* cell_uv,
+                                  QuadSmem& sm) {
+    const int mc = d.max_candidates;
+    {
         float* quad_out = d.quads + (static_cast<int64_t>(fam) * mc + ci) * 8;
         DecodeOut* out = d.decodes + static_cast<int64_t>(fam) * mc + ci;
         if (!quad_ok) {
             if (lane < 8) quad_out[lane] = bdmath::quiet_nan();
             if (lane == 0) out->id = -1;
-            continue;
+            __syncwarp();
+            return;
         }
         const int dim = family_dim(fam);
         for (int iteration = 0; d.refine_edges && iteration < kFitIterations; ++iteration) {
@@ -1892,11 +1906,18 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
         if (lane < 8) quad_out[lane] = sm.q[lane >> 1][lane & 1];
 
         // Decode: the refined quad's rotations, then the hull quad's only
-        // when none of those decoded.
-        int best = decode_rotations_warp(gray, d, stride, fam, &sm.q[0][0], lane, s_uv[fam], sm.raw,
+        // when none of those decoded and refinement moved a corner (an
+        // unmoved quad would decode the same way again).
+        int best = decode_rotations_warp(gray, d, stride, fam, &sm.q[0][0], lane, cell_uv, sm.raw,
                                          sm.sharp, &sm.res);
-        if (best < 0) {
-            best = decode_rotations_warp(gray, d, stride, fam, &sm.hq[0][0], lane, s_uv[fam], sm.raw,
+        bool moved = false;
+        {
+            const float* qa = &sm.q[0][0];
+            const float* qb = &sm.hq[0][0];
+            for (int k = 0; k < 8; ++k) moved = moved || __float_as_uint(qa[k]) != __float_as_uint(qb[k]);
+        }
+        if (best < 0 && moved) {
+            best = decode_rotations_warp(gray, d, stride, fam, &sm.hq[0][0], lane, cell_uv, sm.raw,
                                          sm.sharp, &sm.res);
         }
         if (lane == 0) {
@@ -1921,7 +1942,7 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
 // group per edge), and warps 2s / 2s+1 decode the refined / hull quad of
 // slot s (the hull result is used only when no refined rotation decodes).
 // CTA c takes the big candidates of rank c, c + grid, ... in work-list order.
-__global__ void __launch_bounds__(256) k_fit_decode_big(const BatchDesc* __restrict__ b,
+__global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __restrict__ b,
                                                         const FrameIO* __restrict__ io, int split_px) {
     constexpr int kWarps = 8;
     __shared__ uint32_t boundary[2 * kMaxBoundaryRows];
@@ -2129,13 +2150,23 @@ __global__ void __launch_bounds__(256) k_fit_decode_big(const BatchDesc* __restr
                 d.quads[(static_cast<int64_t>(fam) * mc + ci) * 8 + (tid & 7)] =
                     fit_quad[slot][(tid & 7) >> 1][tid & 1];
             }
+            bool hull_needed = false;  // refinement moved a corner of this warp's slot
             if (warp < 2 * nfam) {
+                const float* qa = &fit_quad[warp >> 1][0][0];
+                const float* qb = &hull_quad[0][0];
+                for (int k = 0; k < 8; ++k) {
+                    hull_needed = hull_needed || __float_as_uint(qa[k]) != __float_as_uint(qb[k]);
+                }
+            }
+            if (warp < 2 * nfam && ((warp & 1) == 0 || hull_needed)) {
                 const int slot = warp >> 1;
                 const float* src = (warp & 1) == 0 ? &fit_quad[slot][0][0] : &hull_quad[0][0];
                 const int best = decode_rotations_warp(gray, d, stride, fam_of_slot[slot], src, lane,
                                                        s_uv[fam_of_slot[slot]], s_raw[warp],
                                                        s_sharp[warp], &s_res[warp]);
                 if (lane == 0) s_best[warp] = best;
+            } else if (warp < 2 * nfam && lane == 0) {
+                s_best[warp] = -1;  // unmoved quad: the refined decode covers it
             }
             __syncthreads();
             if (tid < nfam) {
