@@ -629,10 +629,25 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
         }
         __syncthreads();
 
+        // Flatten the forest by pointer jumping (parents have smaller
+        // indices, so every value written is an ancestor): log-depth rounds
+        // instead of each run walking its whole chain.
+        for (;;) {
+            int changed = 0;
+            for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
+                const uint32_t p = sm_par[i];
+                const uint32_t gp = sm_par[p];
+                if (gp != p) {
+                    sm_par[i] = gp;
+                    changed = 1;
+                }
+            }
+            if (!__syncthreads_or(changed)) break;
+        }
+
         // Segment roots (its smallest slot) and their area / bbox.
         for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
-            uint32_t r = i;
-            while (sm_par[r] != r) r = sm_par[r];
+            const uint32_t r = sm_par[i];
             int row = 0;
             while (row + 1 < kTile && s_rowoff[row + 1] <= seg_off + i) ++row;
             const uint32_t run = sm_run[i];
