@@ -333,9 +333,11 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
 // ===========================================================================
 constexpr int kMaxBandCap = 2048;
 // Dynamic shared memory of k_binarize_runs: six arrays of `cap` run
-// entries, then the band's bit rows (kTile rows of `words` words).
+// entries, the band's bit rows (kTile rows of `words` words), then the row
+// (byte) of each run entry.
 __host__ __device__ constexpr size_t band_smem_bytes(int cap, int words) {
-    return (6 * static_cast<size_t>(cap) + kTile * static_cast<size_t>(words)) * sizeof(uint32_t);
+    return (6 * static_cast<size_t>(cap) + kTile * static_cast<size_t>(words)) * sizeof(uint32_t) +
+           static_cast<size_t>(cap);
 }
 
 __device__ __forceinline__ uint32_t s_find(uint32_t* par, uint32_t x) {
@@ -374,7 +376,10 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
     uint32_t* sm_maxx = s_dyn + 4 * cap;
     uint32_t* sm_rows = s_dyn + 5 * cap;
     uint32_t* sm_bits = s_dyn + 6 * cap;  // kTile rows of bits_words words
+    uint8_t* sm_row = reinterpret_cast<uint8_t*>(sm_bits + kTile * bits_words);  // cap: row of each run
     __shared__ uint8_t s_thresh[BD_MAX_WIDTH / kTile];
+    __shared__ uint8_t s_vmin[BD_MAX_WIDTH / kTile];
+    __shared__ uint8_t s_vmax[BD_MAX_WIDTH / kTile];
     __shared__ uint32_t s_rowtot[kTile];
     __shared__ uint32_t s_rowoff[kTile + 1];
     __shared__ uint32_t s_nroots;
@@ -418,17 +423,28 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
     const uint32_t ref0 = st->ref[0], ref1 = st->ref[1];
     const int floor_contrast = max(kMinTileContrast, static_cast<int>((ref0 * 3) / 2));
     const int t_end = min(4 * wx_hi + 3, tw - 1);
-    for (int t = 4 * wx_lo + tid; t <= t_end; t += blockDim.x) {
+    // The 3x3 window min/max, separably: columns over the three tile rows
+    // (coalesced loads into shared memory), then three columns.
+    const int c_lo = max(4 * wx_lo - 1, 0), c_hi = min(t_end + 1, tw - 1);
+    for (int xx = c_lo + tid; xx <= c_hi; xx += blockDim.x) {
         int mn = 255, mx = 0;
         for (int dy = -1; dy <= 1; ++dy) {
             const int yy = ty + dy;
             if (yy < 0 || yy >= th) continue;
-            for (int dx = -1; dx <= 1; ++dx) {
-                const int xx = t + dx;
-                if (xx < 0 || xx >= tw) continue;
-                mn = min(mn, static_cast<int>(d.tile_min[yy * tw + xx]));
-                mx = max(mx, static_cast<int>(d.tile_max[yy * tw + xx]));
-            }
+            mn = min(mn, static_cast<int>(d.tile_min[yy * tw + xx]));
+            mx = max(mx, static_cast<int>(d.tile_max[yy * tw + xx]));
+        }
+        s_vmin[xx] = static_cast<uint8_t>(mn);
+        s_vmax[xx] = static_cast<uint8_t>(mx);
+    }
+    __syncthreads();
+    for (int t = 4 * wx_lo + tid; t <= t_end; t += blockDim.x) {
+        int mn = 255, mx = 0;
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int xx = t + dx;
+            if (xx < 0 || xx >= tw) continue;
+            mn = min(mn, static_cast<int>(s_vmin[xx]));
+            mx = max(mx, static_cast<int>(s_vmax[xx]));
         }
         int thr = static_cast<int>(ref1);
         if (mx - mn >= floor_contrast) thr = (mn + mx + 1) >> 1;
@@ -551,6 +567,7 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
                         const uint32_t li = s_rowoff[w] + index;
                         sm_run[li] = packed;
                         sm_par[li] = li;
+                        sm_row[li] = static_cast<uint8_t>(w);
                     } else if (fallback) {
                         // Every run is its own band root.
                         d.parent[id] = id;
@@ -585,6 +602,7 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
                 while (row + 1 < kTile && s_rowoff[row + 1] <= seg_off + i) ++row;
                 sm_run[i] = d.runs[static_cast<int64_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row])];
                 sm_par[i] = i;
+                sm_row[i] = static_cast<uint8_t>(row);
             }
             sm_area[i] = 0u;
             sm_minx[i] = 0xffffffffu;
@@ -648,8 +666,7 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
         // Segment roots (its smallest slot) and their area / bbox.
         for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
             const uint32_t r = sm_par[i];
-            int row = 0;
-            while (row + 1 < kTile && s_rowoff[row + 1] <= seg_off + i) ++row;
+            const int row = sm_row[i];
             const uint32_t run = sm_run[i];
             const uint32_t x0 = run & 0xffffu, x1 = run >> 16;
             atomicAdd(&sm_area[r], x1 - x0 + 1);
@@ -657,8 +674,7 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
             atomicMax(&sm_maxx[r], x1);
             atomicOr(&sm_rows[r], 1u << row);
             // parent link = the local root's slot
-            int rrow = 0;
-            while (rrow + 1 < kTile && s_rowoff[rrow + 1] <= seg_off + r) ++rrow;
+            const int rrow = sm_row[r];
             const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row]);
             const uint32_t rslot = static_cast<uint32_t>(y0 + rrow) * row_cap + (seg_off + r - s_rowoff[rrow]);
             d.parent[slot] = rslot;
@@ -666,8 +682,7 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
         __syncthreads();
         for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
             if (sm_par[i] != i) continue;
-            int row = 0;
-            while (row + 1 < kTile && s_rowoff[row + 1] <= seg_off + i) ++row;
+            const int row = sm_row[i];
             const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row]);
             const uint32_t rm = sm_rows[i];
             d.area[slot] = sm_area[i];
