@@ -119,6 +119,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def aggregate_ranks(elapsed_ms: float, e2e_ms: float, steps: int, world: int, device="cuda"):
+    """Whole-job throughput of `world` replicas: every rank processed
+    steps * BATCH frames, and the job lasts as long as the slowest rank (max
+    over ranks of the device time).  Returns (elapsed_ms, e2e_ms, value,
+    e2e_value) with the maxima."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([elapsed_ms, e2e_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms, e2e_ms = float(t[0]), float(t[1])
+    frames_total = steps * BATCH * world
+    return elapsed_ms, e2e_ms, frames_total / (elapsed_ms * 1e-3), frames_total / (e2e_ms * 1e-3)
+
+
 def pct(values, q):
     return float(np.percentile(np.asarray(values), q)) if len(values) else None
 
@@ -580,8 +603,7 @@ def bench_ours(args, rank, world, local_rank):
     for p, s in zip(plans, streams):
         p.set_stream(s)
 
-    if world > 1:
-        torch.distributed.barrier()
+    barrier(world)
     tuned, tune_trials = None, None
     if args.launch:
         fixed = {k: int(v) for k, v in (kv.split("=") for kv in args.launch.split(","))}
@@ -599,16 +621,13 @@ def bench_ours(args, rank, world, local_rank):
             print(json.dumps({"quick": True, "value": args.steps * BATCH / (elapsed_ms * 1e-3),
                               "unit": "frames/s", "p99_ms": pct(lat, 99)}), flush=True)
         return
+    barrier(world)
     with ClockSampler(local_rank) as clocks:
         elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps, args.warmup, device=True)
+    barrier(world)
     e2e_ms, e2e_lat = run_batched(plans, streams, sets_host, args.steps, args.warmup, device=False)
-    if world > 1:
-        t = torch.tensor([elapsed_ms, e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms, e2e_ms = float(t[0]), float(t[1])
-    frames_total = args.steps * BATCH * world
-    value = frames_total / (elapsed_ms * 1e-3)
-    e2e_value = frames_total / (e2e_ms * 1e-3)
+    barrier(world)
+    elapsed_ms, e2e_ms, value, e2e_value = aggregate_ranks(elapsed_ms, e2e_ms, args.steps, world)
     if rank != 0:
         return
 
