@@ -13,8 +13,9 @@
 //   k_merge          8-connected union-find of runs  <- k_merge_runs :509
 //   k_region_stats   area / bbox per root  <- k_region_stats :562
 //   k_cand_count     root flattening, tag-like filter, ordered per-band
-//                    bin ranks, (last CTA) bin bases <- k_collect_candidates :591
-//   k_cand_emit      ordered flattening into candidates  <- k_order_candidates :642
+//                    bin ranks; the frame's last CTA computes the bin bases
+//                    and places the candidates  <- k_collect_candidates :591,
+//                    k_order_candidates :642
 //   k_fit_decode     warp per candidate: hull, four corners, per-family
 //                    edge refinement and decode  <- k_fit_quads :1081,
 //                    k_decode_quads :1438
@@ -843,6 +844,10 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     __shared__ uint32_t s_run[64];
     __shared__ uint32_t s_chunk[4][64];
     __shared__ uint32_t s_total[64];
+    __shared__ uint32_t s_base[64];
+    __shared__ uint32_t s_cprefix[kMaxBandsPerFrame + 1];  // candidates before each band
+    __shared__ uint32_t s_warp_sum[8];
+    __shared__ uint32_t s_ncand, s_limit;
     __shared__ int s_last;
 
     const int tid = threadIdx.x;
@@ -862,9 +867,13 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
         s_rowoff[kTile] = off;
     }
     if (tid < 64) s_run[tid] = 0;
+    if (tid == 0) s_ncand = 0;
     __syncthreads();
     const uint32_t total = s_rowoff[kTile];
     const int w = tid >> 5, lane = tid & 31;
+    // The band's candidate roots are listed in its lroots range (free since
+    // k_region_stats), for the frame's last CTA to place.
+    uint32_t* band_list = d.lroots + static_cast<int64_t>(ty) * kTile * row_cap;
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         const uint32_t i = base + tid;
         int bin = -1;
@@ -895,11 +904,15 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
             for (int w2 = 0; w2 < 8; ++w2) add += s_wbin[w2][tid];
             s_run[tid] += add;
         }
-        if (i < total) d.cand_meta[slot] = meta;
+        if (bin >= 0) {
+            d.cand_meta[slot] = meta;
+            band_list[atomicAdd(&s_ncand, 1u)] = slot;
+        }
         __syncthreads();  // s_wbin is cleared for the next chunk
     }
     __syncthreads();
     if (tid < 64) d.band_bins[ty * 64 + tid] = s_run[tid];
+    if (tid == 0) d.lroot_count[ty] = s_ncand;
     __threadfence();
     __syncthreads();
     if (tid == 0) s_last = atomicAdd(&st->done_cands, 1u) == static_cast<uint32_t>(d.tile_h - 1);
@@ -933,44 +946,50 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     if (tid == 0) {
         uint32_t pos = 0;
         for (int bin = 0; bin < 64; ++bin) {
+            s_base[bin] = pos;
             st->bin_base[bin] = pos;
             pos += s_total[bin];
         }
         st->counts[0] = pos;
-        st->n_candidates = min(pos, static_cast<uint32_t>(d.max_candidates));
+        s_limit = min(pos, static_cast<uint32_t>(d.max_candidates));
+        st->n_candidates = s_limit;
     }
-}
 
-// ===========================================================================
-// 6. Ordered flattening (reference k_order_candidates :642-654).
-// ===========================================================================
-__global__ void __launch_bounds__(256) k_cand_emit(const BatchDesc* __restrict__ b,
-                                                   const FrameIO* __restrict__ io) {
-    __shared__ uint32_t s_rowoff[kTile + 1];
-    const int fi = frame_of_band(b, blockIdx.x);
-    if (!io[fi].gray) return;  // slot not used in this launch
-    const FrameDesc& d = b->f[fi];
-    const int ty = blockIdx.x - b->band_prefix[fi];
-    const FrameState* st = d.state;
-    const int y0 = ty * kTile;
-    const uint32_t row_cap = static_cast<uint32_t>(d.row_cap);
-    if (threadIdx.x == 0) {
-        uint32_t off = 0;
-        for (int r = 0; r < kTile; ++r) {
-            s_rowoff[r] = off;
-            off += y0 + r < d.height ? d.row_count[y0 + r] : 0u;
-        }
-        s_rowoff[kTile] = off;
+    // Placement (reference k_order_candidates :642-654): candidate j of the
+    // frame, flattened over the bands' lists, goes to bin base + earlier
+    // bands' count in its bin + its rank in the band.  Block scan of the
+    // per-band list lengths first.
+    const int chunk = (th + blockDim.x - 1) / blockDim.x;
+    const int cb0 = min(th, tid * chunk), cb1 = min(th, cb0 + chunk);
+    uint32_t own = 0;
+    for (int band = cb0; band < cb1; ++band) own += __ldcg(&d.lroot_count[band]);
+    uint32_t incl = own;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t v = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += v;
     }
+    if (lane == 31) s_warp_sum[w] = incl;
     __syncthreads();
-    const uint32_t total = s_rowoff[kTile];
-    const uint32_t limit = st->n_candidates;
-    for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
-        const uint32_t slot = band_slot(s_rowoff, y0, row_cap, i);
-        const uint32_t meta = d.cand_meta[slot];
-        if (meta == kNone) continue;
-        const uint32_t bin = meta >> 24;
-        const uint32_t pos = st->bin_base[bin] + d.band_bins[ty * 64 + bin] + (meta & 0xffffffu);
+    uint32_t before = incl - own;
+    for (int w2 = 0; w2 < w; ++w2) before += s_warp_sum[w2];
+    for (int band = cb0; band < cb1; ++band) {
+        s_cprefix[band] = before;
+        before += __ldcg(&d.lroot_count[band]);
+    }
+    if (tid == blockDim.x - 1) s_cprefix[th] = before;
+    __syncthreads();
+    const uint32_t all = s_cprefix[th];
+    const uint32_t limit = s_limit;
+    for (uint32_t j = tid; j < all; j += blockDim.x) {
+        int lo = 0, hi = th - 1;  // last band with s_cprefix[band] <= j
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_cprefix[mid] <= j) lo = mid; else hi = mid - 1;
+        }
+        const uint32_t slot = __ldcg(&d.lroots[static_cast<int64_t>(lo) * kTile * row_cap + (j - s_cprefix[lo])]);
+        const uint32_t meta = __ldcg(&d.cand_meta[slot]);
+        const uint32_t cbin = meta >> 24;
+        const uint32_t pos = s_base[cbin] + __ldcg(&d.band_bins[lo * 64 + cbin]) + (meta & 0xffffffu);
         if (pos < limit) d.candidates[pos] = slot;
     }
 }
@@ -2387,7 +2406,7 @@ int prepare_pipeline() {
 
 const char* const kStageNames[kStageCount] = {
     "stats", "binarize_runs", "merge", "region_stats", "cand_count",
-    "cand_emit", "fit_decode_big", "fit_decode", "finalize"};
+    "fit_decode_big", "fit_decode", "finalize"};
 
 void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* io, void* stream_ptr,
                       const LaunchConfig& lc, int sm_count, const ForkJoin* fork,
@@ -2418,8 +2437,6 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     mark(4);
     k_cand_count<<<bands, 256, 0, s>>>(dd, io);
     mark(5);
-    k_cand_emit<<<bands, 256, 0, s>>>(dd, io);
-    mark(6);
     const int split = lc.quad_split;
     int cands = 0;
     for (int f = 0; f < hd.frames; ++f) cands += hd.f[f].max_candidates;
@@ -2434,16 +2451,16 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
         cudaEventRecord(static_cast<cudaEvent_t>(fork->join_event), s2);
         k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io, split);
         cudaStreamWaitEvent(s, static_cast<cudaEvent_t>(fork->join_event), 0);
+        mark(6);
         mark(7);
-        mark(8);
     } else {
         if (split > 0) k_fit_decode_big<<<big_grid, 256, 0, s>>>(dd, io, split);
-        mark(7);
+        mark(6);
         k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io, split);
-        mark(8);
+        mark(7);
     }
     k_finalize<<<hd.frames * 2, kFinalThreads, 0, s>>>(dd);
-    mark(9);
+    mark(8);
 }
 
 }  // namespace bdgb

@@ -21,6 +21,7 @@
 namespace bdgb {
 
 constexpr int kMaxFrames = 64;         // frames in one batch plan
+constexpr int kMaxBandsPerFrame = BD_MAX_HEIGHT / 8;  // 8-row bands of the tallest frame
 constexpr int kTile = 8;               // tile side, pixels
 constexpr int kMinTileContrast = 12;   // reference gpu_detector.cu:39
 constexpr int kFitDirections = 32;     // :46
@@ -154,7 +155,7 @@ BDGB_HD inline size_t result_bytes(int max_detections) {
 // stage_events is not null (no fork then) it holds kStageCount + 1
 // cudaEvent_t, recorded before the first kernel and after every kernel, so
 // consecutive events bracket one stage.
-constexpr int kStageCount = 9;
+constexpr int kStageCount = 8;
 // Per-device kernel attributes; call with the device current before the
 // first enqueue.  0 on success.
 int prepare_pipeline();

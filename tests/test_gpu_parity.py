@@ -276,7 +276,7 @@ def test_batch_pinned_stream_query_profile():
     batch.set_stream(None)
     dev = [torch.from_numpy(f).cuda() for f in frames]
     prof = batch.profile_device(dev, [1280] * 4)
-    assert len(prof) == 9 and all(v >= 0 for v in prof.values())
+    assert len(prof) == 8 and all(v >= 0 for v in prof.values())
     f4, o4 = batch.wait()
     assert np.array_equal(found, f4)
     for i in range(4):
