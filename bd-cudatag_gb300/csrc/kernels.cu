@@ -994,6 +994,41 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     }
 }
 
+// Image homography of a decoded tag's corners (reference host
+// fill_homography :1739-1774, FP64 as there).  Computed by the warp that
+// decodes the candidate, so k_finalize only copies it.
+__device__ void fill_homography(const float corners[8], float H[9]) {
+    const double x0 = corners[0], y0 = corners[1];
+    const double x1 = corners[2], y1 = corners[3];
+    const double x2 = corners[4], y2 = corners[5];
+    const double x3 = corners[6], y3 = corners[7];
+    const double dx1 = x1 - x2, dx2 = x3 - x2;
+    const double dx3 = x0 - x1 + x2 - x3;
+    const double dy1 = y1 - y2, dy2 = y3 - y2;
+    const double dy3 = y0 - y1 + y2 - y3;
+    double g = 0.0, h = 0.0;
+    const double det = dx1 * dy2 - dx2 * dy1;
+    if (fabs(det) > 1e-12) {
+        g = (dx3 * dy2 - dx2 * dy3) / det;
+        h = (dx1 * dy3 - dx3 * dy1) / det;
+    }
+    const double a = x1 - x0 + g * x1;
+    const double bb = x3 - x0 + h * x3;
+    const double dd = y1 - y0 + g * y1;
+    const double e = y3 - y0 + h * y3;
+    const double w = g + h + 2.0;
+    const double inv = (fabs(w) > 1e-12) ? 1.0 / w : 0.0;
+    H[0] = static_cast<float>(a * inv);
+    H[1] = static_cast<float>(bb * inv);
+    H[2] = static_cast<float>((a + bb + 2.0 * x0) * inv);
+    H[3] = static_cast<float>(dd * inv);
+    H[4] = static_cast<float>(e * inv);
+    H[5] = static_cast<float>((dd + e + 2.0 * y0) * inv);
+    H[6] = static_cast<float>(g * inv);
+    H[7] = static_cast<float>(h * inv);
+    H[8] = static_cast<float>(w * inv);
+}
+
 // ===========================================================================
 // 7. Quad fit (reference k_fit_quads :1081-1241 and helpers :659-1076).
 // ===========================================================================
@@ -1977,6 +2012,10 @@ __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uin
                 out->hamming = sm.res.hamming;
                 out->margin = sm.res.margin;
                 for (int k = 0; k < 8; ++k) out->corners[k] = sm.res.corners[k];
+                float hm[9];
+                fill_homography(sm.res.corners, hm);
+                float* hout = d.dec_h + (static_cast<int64_t>(fam) * mc + ci) * 9;
+                for (int k = 0; k < 9; ++k) hout[k] = hm[k];
             }
         }
         __syncwarp();
@@ -2228,6 +2267,10 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
                     out->hamming = s_res[pick].hamming;
                     out->margin = s_res[pick].margin;
                     for (int k = 0; k < 8; ++k) out->corners[k] = s_res[pick].corners[k];
+                    float hm[9];
+                    fill_homography(s_res[pick].corners, hm);
+                    float* hout = d.dec_h + (static_cast<int64_t>(fam_of_slot[tid]) * mc + ci) * 9;
+                    for (int k = 0; k < 9; ++k) hout[k] = hm[k];
                 }
             }
             __syncthreads();
@@ -2244,43 +2287,13 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
 //    (reference k_finalize :1542-1601, host fill_homography :1739-1774 --
 //    FP64 here as there).
 // ===========================================================================
-__device__ void fill_homography(const float corners[8], float H[9]) {
-    const double x0 = corners[0], y0 = corners[1];
-    const double x1 = corners[2], y1 = corners[3];
-    const double x2 = corners[4], y2 = corners[5];
-    const double x3 = corners[6], y3 = corners[7];
-    const double dx1 = x1 - x2, dx2 = x3 - x2;
-    const double dx3 = x0 - x1 + x2 - x3;
-    const double dy1 = y1 - y2, dy2 = y3 - y2;
-    const double dy3 = y0 - y1 + y2 - y3;
-    double g = 0.0, h = 0.0;
-    const double det = dx1 * dy2 - dx2 * dy1;
-    if (fabs(det) > 1e-12) {
-        g = (dx3 * dy2 - dx2 * dy3) / det;
-        h = (dx1 * dy3 - dx3 * dy1) / det;
-    }
-    const double a = x1 - x0 + g * x1;
-    const double bb = x3 - x0 + h * x3;
-    const double dd = y1 - y0 + g * y1;
-    const double e = y3 - y0 + h * y3;
-    const double w = g + h + 2.0;
-    const double inv = (fabs(w) > 1e-12) ? 1.0 / w : 0.0;
-    H[0] = static_cast<float>(a * inv);
-    H[1] = static_cast<float>(bb * inv);
-    H[2] = static_cast<float>((a + bb + 2.0 * x0) * inv);
-    H[3] = static_cast<float>(dd * inv);
-    H[4] = static_cast<float>(e * inv);
-    H[5] = static_cast<float>((dd + e + 2.0 * y0) * inv);
-    H[6] = static_cast<float>(g * inv);
-    H[7] = static_cast<float>(h * inv);
-    H[8] = static_cast<float>(w * inv);
-}
 
 constexpr int kFinalThreads = 256;
 
 __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __restrict__ b) {
     __shared__ DecodeOut s_in[kMaxDetectionsCap];
     __shared__ DecodeOut s_out[kMaxDetectionsCap];
+    __shared__ int s_in_src[kMaxDetectionsCap], s_out_src[kMaxDetectionsCap];  // candidate index
     __shared__ float s_cx[kMaxDetectionsCap], s_cy[kMaxDetectionsCap];
     __shared__ uint32_t s_warp[kFinalThreads / 32];
     __shared__ int s_count, s_kept;
@@ -2312,7 +2325,10 @@ __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __r
         int before = s_count;
         for (int w2 = 0; w2 < warp; ++w2) before += static_cast<int>(s_warp[w2]);
         const int pos = before + __popc(bal & lanemask_lt());
-        if (ok && pos < maxd) s_in[pos] = dec[i];
+        if (ok && pos < maxd) {
+            s_in[pos] = dec[i];
+            s_in_src[pos] = i;
+        }
         __syncthreads();
         if (tid == 0) {
             int add = 0;
@@ -2353,11 +2369,13 @@ __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __r
                 if (duplicate >= 0) {
                     if (dd.margin > s_out[duplicate].margin) {
                         s_out[duplicate] = dd;
+                        s_out_src[duplicate] = s_in_src[i];
                         s_cx[duplicate] = cx;
                         s_cy[duplicate] = cy;
                     }
                 } else if (kept < maxd) {
                     s_out[kept] = dd;
+                    s_out_src[kept] = s_in_src[i];
                     s_cx[kept] = cx;
                     s_cy[kept] = cy;
                 }
@@ -2383,7 +2401,8 @@ __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __r
         r.decision_margin = s_out[i].margin;
         for (int k = 0; k < 8; ++k) r.corners[k] = s_out[i].corners[k];
         r.reserved = 0;
-        fill_homography(r.corners, r.homography);
+        const float* hsrc = d.dec_h + (static_cast<int64_t>(fam) * d.max_candidates + s_out_src[i]) * 9;
+        for (int k = 0; k < 9; ++k) r.homography[k] = hsrc[k];
         dets[rank] = r;
     }
     if (tid == 0) hdr->found[fam] = static_cast<uint32_t>(kept);
