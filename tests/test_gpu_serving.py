@@ -9,7 +9,7 @@ import scenes
 
 pytestmark = pytest.mark.gpu
 
-CAMS = [(640, 480, 3), (1280, 800, 3), (1920, 1080, 1), (1600, 1304, 2)]
+CAMS = [(640, 480, 3), (1280, 800, 3), (1920, 1080, 1), (1600, 1304, 2), (3840, 2160, 3)]
 
 
 def alone(frame, w, h, fams):
