@@ -419,15 +419,31 @@ int Plan::submit_host(const uint8_t* const* frames, const int32_t* strides, std:
     if (!any_direct) {
         im.launch(0, s);
     } else {
-        for (int i = 0; i < this->frames(); ++i) {
+        for (int i = 0; i < this->frames();) {
             const int w = frames_[i].width, h = frames_[i].height;
             uint8_t* dev = im.frames_dev + im.frame_offset[i];
+            if (direct[i] && strides[i] == w) {
+                // Tightly strided frames that follow one another both in the
+                // caller's memory and in the plan's buffer go in one copy.
+                size_t bytes = static_cast<size_t>(w) * h;
+                int j = i + 1;
+                while (j < this->frames() && direct[j] && strides[j] == frames_[j].width &&
+                       frames[j] == frames[i] + bytes &&
+                       im.frame_offset[j] == im.frame_offset[i] + bytes) {
+                    bytes += static_cast<size_t>(frames_[j].width) * frames_[j].height;
+                    ++j;
+                }
+                cudaMemcpyAsync(dev, frames[i], bytes, cudaMemcpyHostToDevice, s);
+                i = j;
+                continue;
+            }
             if (direct[i]) {
                 cudaMemcpy2DAsync(dev, w, frames[i], strides[i], w, h, cudaMemcpyHostToDevice, s);
             } else {
                 cudaMemcpyAsync(dev, im.frames_pinned + im.frame_offset[i], static_cast<size_t>(w) * h,
                                 cudaMemcpyHostToDevice, s);
             }
+            ++i;
         }
         im.launch(1, s);
     }
