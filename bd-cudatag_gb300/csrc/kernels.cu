@@ -736,7 +736,7 @@ __device__ __forceinline__ void merge_run_with_row_above(uint32_t* parent, const
 }
 
 __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b,
-                                               const FrameIO* __restrict__ io) {
+                                               const FrameIO* __restrict__ io, int row_cap_max) {
     const int fi = frame_of_band(b, blockIdx.x);
     if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
@@ -747,19 +747,27 @@ __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b,
     if (!(mode & 1u)) {
         // Band-local unions are done: the first row of the band, and the
         // first row of every further segment (bit r of the mode), meet the
-        // row above; their runs are spread over the whole CTA.
+        // row above.  Both rows are staged in shared memory (the searches
+        // run there); their runs are spread over the whole CTA.
+        extern __shared__ __align__(16) uint32_t s_dyn[];
+        uint32_t* s_prev = s_dyn;
+        uint32_t* s_cur = s_dyn + row_cap_max;
         for (uint32_t starts = mode | 1u; starts; starts &= starts - 1u) {
             const int y = ty * kTile + __ffs(starts) - 1;
-            if (y <= 0 || y >= d.height) continue;
+            if (y <= 0 || y >= d.height) continue;  // uniform over the CTA
             const int n = static_cast<int>(d.row_count[y]);
             const int prev_n = static_cast<int>(d.row_count[y - 1]);
             const uint32_t* cur = d.runs + static_cast<int64_t>(y) * row_cap;
             const uint32_t* prev = d.runs + static_cast<int64_t>(y - 1) * row_cap;
+            for (int i = threadIdx.x; i < prev_n; i += blockDim.x) s_prev[i] = prev[i];
+            for (int i = threadIdx.x; i < n; i += blockDim.x) s_cur[i] = cur[i];
+            __syncthreads();
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                merge_run_with_row_above(parent, cur, prev, i, prev_n,
+                merge_run_with_row_above(parent, s_cur, s_prev, i, prev_n,
                                          static_cast<uint32_t>(y * row_cap),
                                          static_cast<uint32_t>((y - 1) * row_cap), false);
             }
+            __syncthreads();  // the next pair reuses the buffers
         }
         return;
     }
@@ -2450,7 +2458,9 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     k_binarize_runs<<<bands, 256, band_smem_bytes(lc.band_cap, words_max), s>>>(dd, io, lc.band_cap,
                                                                                  words_max);
     mark(2);
-    k_merge<<<bands, 256, 0, s>>>(dd, io);
+    int row_cap_max = 1;
+    for (int f = 0; f < hd.frames; ++f) row_cap_max = std::max(row_cap_max, hd.f[f].row_cap);
+    k_merge<<<bands, 256, 2 * row_cap_max * sizeof(uint32_t), s>>>(dd, io, row_cap_max);
     mark(3);
     k_region_stats<<<bands, 256, 0, s>>>(dd, io);
     mark(4);
