@@ -12,8 +12,8 @@
 //    [-3, 3]).  The steps have to be the same to give the same pixels; the
 //    tests compare SHA-256 hashes of these frames with frames written by the
 //    reference's own scene exporter.
-//  * bds_render_config: this project's seeded generator for the five
-//    workload configurations (gradient background, Gaussian-like noise, both
+//  * bds_render_scene: this project's seeded generator for the five
+//    workload scene sets (gradient background, Gaussian-like noise, both
 //    families, perspective tilt, blur, decoys, glyph clutter).  It uses only
 //    integer arithmetic and IEEE double +, -, *, /, sqrt (own sin/cos), so a
 //    seed gives the same frame on x86 and Arm.
@@ -534,9 +534,9 @@ int render_scene(const SceneSpec& spec, uint64_t seed, int width, int height, ui
     return count;
 }
 
-SceneSpec spec_for(int config, int frame_index, Rng& choose) {
+SceneSpec spec_for(int scene_set, int frame_index, Rng& choose) {
     SceneSpec s;
-    switch (config) {
+    switch (scene_set) {
         case 1:
             break;
         case 2:
@@ -655,23 +655,23 @@ __attribute__((visibility("default"))) int bds_ref_scenes(int width, int height,
     return 0;
 }
 
-// One frame of workload configuration `config` (1, 2, 3, 4 or 5) with the
+// One frame of scene set `scene_set` (1, 2, 3, 4 or 5) with the
 // given seed.  Returns the number of real tags written to `tags` (each 72
 // bytes: family, id, 4 corners as doubles).
-__attribute__((visibility("default"))) int bds_render_config(int config, uint64_t seed,
+__attribute__((visibility("default"))) int bds_render_scene(int scene_set, uint64_t seed,
                                                              int frame_index, int width, int height,
                                                              uint8_t* image, void* tags, int max_tags) {
     if (!image || width < 16 || height < 16) return -1;
     Rng choose{splitmix64(seed * 0x2545f4914f6cdd1dull + 17)};
-    const SceneSpec spec = spec_for(config, frame_index, choose);
+    const SceneSpec spec = spec_for(scene_set, frame_index, choose);
     return render_scene(spec, seed, width, height, image, static_cast<Tag*>(tags), max_tags);
 }
 
-// Renders frames [0, count) of a configuration on `threads` host threads:
+// Renders frames [0, count) of a scene set on `threads` host threads:
 // frame i uses seed base_seed + i and size widths[i] x heights[i], packed
 // back to back into images.  tag_counts[i] receives the tag count and tags
 // gets max_tags records per frame.
-__attribute__((visibility("default"))) int bds_render_many(int config, uint64_t base_seed, int count,
+__attribute__((visibility("default"))) int bds_render_many(int scene_set, uint64_t base_seed, int count,
                                                            const int32_t* widths,
                                                            const int32_t* heights, uint8_t* images,
                                                            void* tags, int max_tags,
@@ -685,8 +685,8 @@ __attribute__((visibility("default"))) int bds_render_many(int config, uint64_t 
     for (int t = 0; t < n; ++t) {
         pool.emplace_back([&, t]() {
             for (int i = t; i < count; i += n) {
-                tag_counts[i] = bds_render_config(
-                    config, base_seed + static_cast<uint64_t>(i), i, widths[i], heights[i],
+                tag_counts[i] = bds_render_scene(
+                    scene_set, base_seed + static_cast<uint64_t>(i), i, widths[i], heights[i],
                     images + offsets[i], static_cast<Tag*>(tags) + static_cast<size_t>(i) * max_tags,
                     max_tags);
             }

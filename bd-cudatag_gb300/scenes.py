@@ -1,13 +1,16 @@
 """Seeded synthetic frames with ground truth (ctypes over libbdscenes.so).
 
-Workload configurations follow the benchmark definition of this project:
-  1  640x480, 8 tag36h11 tags, side 40-120 px, noise sigma 4, tilt <= 45 deg
-  2  1280x800, 6 tag36h11 + 2 tag16h5, side 20-200 px, sigma 6, blur on odd
-     frames, two decoys on frames i % 4 == 3, glyph clutter on i % 8 == 5
-  3  mixed sizes, 4-24 tags of both families, side 16-300 px, sigma 2-8
-  4  as 2 (frames for the corner-refinement workload)
-  5  serving mix: 0-40 tags, 10% blank frames, sigma 2-8
-Config k uses base seed 6324 + 1000*k and frame i uses seed base + i.
+Scene sets (the `scene_set` argument), with the benchmark workloads they feed:
+  EIGHT_TAGS_640  640x480, 8 tag36h11 tags, side 40-120 px, noise sigma 4,
+                  tilt <= 45 deg (the reference-style single-frame scenes)
+  MIXED_1280      1280x800, 6 tag36h11 + 2 tag16h5, side 20-200 px, sigma 6,
+                  blur on odd frames, two decoys on frames i % 4 == 3, glyph
+                  clutter past the candidate cap on i % 8 == 5
+  MULTI_SIZE      any size, 4-24 tags of both families, side 16-300 px,
+                  sigma 2-8 (16-frame batches of uneven sizes)
+  REFINE_1280     as MIXED_1280, own seeds (corner-refinement quads)
+  SERVING         0-40 tags, 10% blank frames, sigma 2-8 (camera streams)
+Set k uses base seed 6324 + 1000*k and frame i uses seed base + i.
 """
 from __future__ import annotations
 
@@ -19,10 +22,11 @@ import numpy as np
 
 _LIB = None
 MAX_TAGS = 64
+EIGHT_TAGS_640, MIXED_1280, MULTI_SIZE, REFINE_1280, SERVING = 1, 2, 3, 4, 5
 
 
-def base_seed(config: int) -> int:
-    return 6324 + 1000 * config
+def base_seed(scene_set: int) -> int:
+    return 6324 + 1000 * scene_set
 
 
 class _Tag(ctypes.Structure):
@@ -43,7 +47,7 @@ def lib() -> ctypes.CDLL:
                                         ctypes.c_void_p]
         _LIB.bds_ref_scenes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
-        _LIB.bds_render_config.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+        _LIB.bds_render_scene.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_int]
         _LIB.bds_render_many.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
@@ -95,18 +99,18 @@ class TagTruth:
     corners: np.ndarray  # (4, 2), pixel-index convention
 
 
-def render_config(config: int, index: int, width: int, height: int,
+def render_scene(scene_set: int, index: int, width: int, height: int,
                   seed: int | None = None) -> tuple[np.ndarray, list[TagTruth]]:
     img = np.empty((height, width), dtype=np.uint8)
     tags = (_Tag * MAX_TAGS)()
-    s = base_seed(config) + index if seed is None else seed
-    n = lib().bds_render_config(config, s, index, width, height, img.ctypes.data, tags, MAX_TAGS)
+    s = base_seed(scene_set) + index if seed is None else seed
+    n = lib().bds_render_scene(scene_set, s, index, width, height, img.ctypes.data, tags, MAX_TAGS)
     truth = [TagTruth(tags[i].family, tags[i].id, np.array(tags[i].corners).reshape(4, 2))
              for i in range(n)]
     return img, truth
 
 
-def render_many(config: int, sizes: list[tuple[int, int]], threads: int = 8,
+def render_many(scene_set: int, sizes: list[tuple[int, int]], threads: int = 8,
                 base: int | None = None):
     """Renders len(sizes) frames (frame i with seed base + i) on host threads.
 
@@ -120,8 +124,8 @@ def render_many(config: int, sizes: list[tuple[int, int]], threads: int = 8,
     packed = np.empty(total, dtype=np.uint8)
     tags = (_Tag * (MAX_TAGS * count))()
     counts = np.zeros(count, dtype=np.int32)
-    b = base_seed(config) if base is None else base
-    lib().bds_render_many(config, b, count, widths.ctypes.data, heights.ctypes.data,
+    b = base_seed(scene_set) if base is None else base
+    lib().bds_render_many(scene_set, b, count, widths.ctypes.data, heights.ctypes.data,
                           packed.ctypes.data, tags, MAX_TAGS, counts.ctypes.data, threads)
     frames = []
     off = 0

@@ -49,7 +49,7 @@ W, H = 1280, 800
 POOL = 600
 BATCH = 4
 FAMILIES = 3  # both families
-WORKLOAD = ("config2: 4-camera batches of 1280x800 uint8 frames, tag36h11+tag16h5 decoded per "
+WORKLOAD = ("4-camera batches of 1280x800 uint8 frames, tag36h11+tag16h5 decoded per "
             "frame, 600 seeded frames (6 tag36h11 + 2 tag16h5, side 20-200 px, sigma 6, blur on "
             "odd frames, decoys on i%4==3, glyph clutter past the candidate cap on i%8==5)")
 
@@ -62,8 +62,8 @@ def dist_info():
 def render_pool(count: int, offset: int = 0):
     import scenes
 
-    frames, truth = scenes.render_many(2, [(W, H)] * count, threads=os.cpu_count() or 8,
-                                       base=scenes.base_seed(2) + offset)
+    frames, truth = scenes.render_many(scenes.MIXED_1280, [(W, H)] * count, threads=os.cpu_count() or 8,
+                                       base=scenes.base_seed(scenes.MIXED_1280) + offset)
     return frames, truth
 
 
@@ -288,11 +288,11 @@ def serving_trace(seconds: float, seed: int = 6324 + 5000):
     return cams, arrivals
 
 
-CONFIG3_SIZES = [(640, 480), (1280, 800), (1600, 1304), (1920, 1080)] * 4
+MIXED_SIZES = [(640, 480), (1280, 800), (1600, 1304), (1920, 1080)] * 4
 
 
-def measure_config3(steps: int, streams: int = 4, pool_batches: int = 8):
-    """Config 3: 16-frame batches of uneven sizes (4 each of 640x480, 1280x800,
+def measure_mixed_batches(steps: int, streams: int = 4, pool_batches: int = 8):
+    """16-frame batches of uneven sizes (4 each of 640x480, 1280x800,
     1600x1304, 1920x1080), both families, autotuned launch shapes; frames/s
     with frames resident in HBM, and a bit-exact check of one batch against
     single-frame detection."""
@@ -301,13 +301,13 @@ def measure_config3(steps: int, streams: int = 4, pool_batches: int = 8):
     import bdcudatag
     import scenes
 
-    sizes = CONFIG3_SIZES * pool_batches
-    frames, _ = scenes.render_many(3, sizes, threads=os.cpu_count() or 8)
+    sizes = MIXED_SIZES * pool_batches
+    frames, _ = scenes.render_many(scenes.MULTI_SIZE, sizes, threads=os.cpu_count() or 8)
     dev = [torch.from_numpy(f).cuda() for f in frames]
-    nb = len(CONFIG3_SIZES)
+    nb = len(MIXED_SIZES)
     sets = [dev[k * nb:(k + 1) * nb] for k in range(pool_batches)]
-    strides = [w for w, _ in CONFIG3_SIZES]
-    cams = [(w, h, FAMILIES) for w, h in CONFIG3_SIZES]
+    strides = [w for w, _ in MIXED_SIZES]
+    cams = [(w, h, FAMILIES) for w, h in MIXED_SIZES]
     plans = [bdcudatag.Batch(cams) for _ in range(streams)]
     default_launch = plans[0].launch()
     latency_best, tuned_ms = plans[0].autotune(sets[0], strides, iterations=10)
@@ -321,11 +321,11 @@ def measure_config3(steps: int, streams: int = 4, pool_batches: int = 8):
     found, out = plans[0].detect(sets[1], strides, device=True)
     exact = True
     for i in range(nb):
-        w, h = CONFIG3_SIZES[i]
+        w, h = MIXED_SIZES[i]
         for fam in (0, 1):
             n, d = bdcudatag.Detector(fam, w, h).detect(frames[nb + i])
             exact = exact and found[i, fam] == n and out[i, fam, :n].tobytes() == d.tobytes()
-    batch_bytes = sum(w * h for w, h in CONFIG3_SIZES)
+    batch_bytes = sum(w * h for w, h in MIXED_SIZES)
     return {"frames_per_s": round(steps * nb / (elapsed * 1e-3), 2), "batch_frames": nb,
             "batch_bytes": batch_bytes, "streams": streams, "steps": steps,
             "p50_ms": round(pct(lat, 50), 4), "p99_ms": round(pct(lat, 99), 4),
@@ -335,7 +335,8 @@ def measure_config3(steps: int, streams: int = 4, pool_batches: int = 8):
 
 
 def measure_serving(seconds: float, pool_per_cam: int = 12):
-    """Config 5: continuous batching through bd_server versus a FIFO plain
+    """Six camera streams (Poisson arrivals at 60-120 fps each, sizes from
+    640x480 to 3840x2160): continuous batching through bd_server versus a FIFO plain
     per-frame detector fed by the same arrivals."""
     import torch
 
@@ -345,8 +346,8 @@ def measure_serving(seconds: float, pool_per_cam: int = 12):
     cams, arrivals = serving_trace(seconds)
     pools = []
     for c, (w, h, _, _) in enumerate(cams):
-        imgs, _ = scenes.render_many(5, [(w, h)] * pool_per_cam, threads=os.cpu_count() or 8,
-                                     base=scenes.base_seed(5) + 1000 * c)
+        imgs, _ = scenes.render_many(scenes.SERVING, [(w, h)] * pool_per_cam, threads=os.cpu_count() or 8,
+                                     base=scenes.base_seed(scenes.SERVING) + 1000 * c)
         pinned = torch.empty((pool_per_cam, h, w), dtype=torch.uint8, pin_memory=True)
         pinned.numpy()[:] = np.stack(imgs)
         pools.append((imgs, pinned))
@@ -425,7 +426,7 @@ def measure_serving(seconds: float, pool_per_cam: int = 12):
 
 
 def measure_refine(n_quads: int = 256, iterations: int = 5):
-    """Config 4: photometric Gauss-Newton on detected quads of 1280x800
+    """Corner refinement: photometric Gauss-Newton on detected quads of 1280x800
     frames, corners perturbed by U(-1.5, 1.5) px; corner error against ground
     truth before and after, and the kernel times (CUDA events)."""
     import itertools
@@ -452,7 +453,7 @@ def measure_refine(n_quads: int = 256, iterations: int = 5):
     dets = [bdcudatag.Detector(f, W, H) for f in (0, 1)]
     fi = 0
     while sum(len(g["c"]) for g in groups.values()) < n_quads and fi < 200:
-        img, tags = scenes.render_config(4, fi, W, H)
+        img, tags = scenes.render_scene(scenes.REFINE_1280, fi, W, H)
         for fam in (0, 1):
             n, d = dets[fam].detect(img)
             for k in range(n):
@@ -534,7 +535,7 @@ def measure_cpu_baseline(frames, seconds_budget=12.0):
     cpu_s = time.process_time() - c0
     return {"value": round(multi, 2), "unit": "frames/s", "cores": cores, "kind": "port",
             "single_thread": round(single, 2),
-            "sample": f"{n} config2 1280x800 frames (cycling {len(frames)} seeded frames), both "
+            "sample": f"{n} 1280x800 frames of the workload (cycling {len(frames)} seeded frames), both "
                       f"families, oracle on {cores} threads, plus {n1} frames on 1 thread; "
                       f"{cpu_s:.1f} s of CPU time"}
 
@@ -568,7 +569,7 @@ def bench_reference(args, rank):
         "p50_ms": pct(times, 50), "p99_ms": pct(times, 99),
         "config": {"workload": WORKLOAD, "batch_frames": step_frames, "frames_pool": 64},
         "cpu_baseline": {"value": round(value, 2), "unit": "frames/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} steps of {step_frames} config2 frames (both "
+                         "sample": f"{args.steps} steps of {step_frames} 1280x800 workload frames (both "
                                    f"families) from 64 seeded frames"},
         "e2e": {"value": round(value, 2), "unit": "frames/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -647,7 +648,7 @@ def bench_ours(args, rank, world, local_rank):
     cpu = measure_cpu_baseline(frames)
     serving = measure_serving(args.serving_seconds) if args.serving_seconds > 0 else None
     refine = measure_refine()
-    config3 = measure_config3(max(200, args.steps // 5), streams=args.streams)
+    mixed = measure_mixed_batches(max(200, args.steps // 5), streams=args.streams)
     result_bytes = BATCH * ((32 + 2 * plans[0].max_detections * 84 + 255) // 256 * 256)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
@@ -672,7 +673,7 @@ def bench_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "serving": serving,
         "refine": refine,
-        "config3": config3,
+        "mixed_size_batches": mixed,
         "clocks": clocks.summary(),
         "gpu_launches": 9 * args.steps,
     }
@@ -688,7 +689,7 @@ def main():
     ap.add_argument("--streams", type=int, default=8)
     ap.add_argument("--plain-frames", type=int, default=300)
     ap.add_argument("--serving-seconds", type=float, default=60.0,
-                    help="length of the config-5 serving run (0: skip)")
+                    help="length of the six-camera serving run (0: skip)")
     ap.add_argument("--tune", action="store_true", help="tune launch shapes in --quick runs")
     ap.add_argument("--launch", default="",
                     help="fixed launch shapes instead of tuning, e.g. band_cap=1024,quad_split=48")

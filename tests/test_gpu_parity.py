@@ -172,15 +172,15 @@ def test_reference_scenes(w, h):
 # --- workload frames and edge cases -------------------------------------------
 
 @pytest.mark.parametrize("index", range(8))
-def test_config2_frames_both_families(index):
-    img, truth = scenes.render_config(2, index, 1280, 800)
+def test_mixed_1280_frames_both_families(index):
+    img, truth = scenes.render_scene(scenes.MIXED_1280, index, 1280, 800)
     for fam in (0, 1):
         check_frame(img, fam, stages=(index % 4 == 0 or index == 5))
 
 
 @pytest.mark.parametrize("w,h", [(16, 16), (17, 23), (1001, 777), (33, 300), (2000, 40)])
 def test_odd_sizes(w, h):
-    img, _ = scenes.render_config(3, w * 7 + h, w, h)
+    img, _ = scenes.render_scene(scenes.MULTI_SIZE, w * 7 + h, w, h)
     check_frame(img, 0)
     check_frame(np.ascontiguousarray(img[::-1]), 1)
 
@@ -189,7 +189,7 @@ def test_dense_bands_4k():
     # 3840x2160 serving frames hold 8-row bands of up to ~5000 runs: more
     # than one shared-memory segment (default cap 2048), so those bands are
     # labelled in row segments joined by k_merge.
-    img, _ = scenes.render_config(5, 0, 3840, 2160)
+    img, _ = scenes.render_scene(scenes.SERVING, 0, 3840, 2160)
     h, w = img.shape
     rc = oracle.Frame(img, 0).stage("row_count").astype(np.int64)
     pad = np.zeros(((h + 7) // 8) * 8, np.int64)
@@ -223,7 +223,7 @@ def test_single_row_over_cap_fallback():
 def test_caps_exceeded():
     # Clutter frame (index 5) pushes candidates past a small cap; a tiny
     # detection cap truncates in candidate order.
-    img, _ = scenes.render_config(2, 5, 1280, 800)
+    img, _ = scenes.render_scene(scenes.MIXED_1280, 5, 1280, 800)
     check_frame(img, 0, bdcudatag.default_config(max_candidates=16, max_detections=2),
                 oracle.default_config(max_candidates=16, max_detections=2))
     det = bdcudatag.Detector(0, 1280, 800, bdcudatag.default_config(max_detections=4))
@@ -233,7 +233,7 @@ def test_caps_exceeded():
 
 def test_batch_matches_single_frames():
     sizes = [(640, 480), (1280, 800), (1600, 1304), (1920, 1080)] * 2
-    frames, _ = scenes.render_many(3, sizes, threads=8)
+    frames, _ = scenes.render_many(scenes.MULTI_SIZE, sizes, threads=8)
     cams = [(w, h, 3 if i % 3 else 1) for i, (w, h) in enumerate(sizes)]
     batch = bdcudatag.Batch(cams)
     found, out = batch.detect(frames)
@@ -259,7 +259,7 @@ def test_batch_matches_single_frames():
 def test_batch_pinned_stream_query_profile():
     torch = pytest.importorskip("torch")
     sizes = [(1280, 800)] * 4
-    frames, _ = scenes.render_many(2, sizes, threads=8)
+    frames, _ = scenes.render_many(scenes.MIXED_1280, sizes, threads=8)
     pinned = torch.empty((4, 800, 1280), dtype=torch.uint8, pin_memory=True)
     pinned.numpy()[:] = np.stack(frames)
     batch = bdcudatag.Batch([(1280, 800, 3)] * 4)
@@ -289,7 +289,7 @@ def test_batch_pinned_stream_query_profile():
 def test_launch_shapes_and_autotune_keep_results():
     torch = pytest.importorskip("torch")
     sizes = [(640, 480), (1280, 800), (1600, 1304), (1920, 1080)] * 4
-    frames, _ = scenes.render_many(3, sizes, threads=8, base=scenes.base_seed(3) + 500)
+    frames, _ = scenes.render_many(scenes.MULTI_SIZE, sizes, threads=8, base=scenes.base_seed(scenes.MULTI_SIZE) + 500)
     dev = [torch.from_numpy(f).cuda() for f in frames]
     strides = [w for w, _ in sizes]
     batch = bdcudatag.Batch([(w, h, 3) for w, h in sizes])

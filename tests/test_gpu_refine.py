@@ -21,13 +21,13 @@ S = 8  # samples per cell side
 
 
 def detected_quads(frame_indices, max_quads):
-    """Detected quads of config-4 frames matched to ground truth:
+    """Detected quads of 1280x800 refinement frames matched to ground truth:
     (frames uint8 [F,H,W], corners [n,8], truth [n,8], templates [n,C,C] (C=10),
     image_index [n]); tag36h11 only so every template has 10 cells."""
     frames, corners, truth, templates, index = [], [], [], [], []
     det = bdcudatag.Detector(0, 1280, 800)
     for fi in frame_indices:
-        img, tags = scenes.render_config(4, fi, 1280, 800)
+        img, tags = scenes.render_scene(scenes.REFINE_1280, fi, 1280, 800)
         n, d = det.detect(img)
         for k in range(n):
             for t in tags:

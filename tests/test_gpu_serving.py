@@ -26,7 +26,7 @@ def test_results_same_alone_and_in_mix():
     per_cam = 5
     frames = {}
     for c, (w, h, _) in enumerate(CAMS):
-        imgs, _ = scenes.render_many(5, [(w, h)] * per_cam, base=scenes.base_seed(5) + 100 * c)
+        imgs, _ = scenes.render_many(scenes.SERVING, [(w, h)] * per_cam, base=scenes.base_seed(scenes.SERVING) + 100 * c)
         pinned = torch.empty((per_cam, h, w), dtype=torch.uint8, pin_memory=True)
         pinned.numpy()[:] = np.stack(imgs)
         frames[c] = (imgs, pinned)
@@ -62,7 +62,7 @@ def test_results_same_alone_and_in_mix():
 
 def test_admission_and_rejection():
     w, h, fams = 640, 480, 1
-    img, _ = scenes.render_config(5, 3, w, h)
+    img, _ = scenes.render_scene(scenes.SERVING, 3, w, h)
     # A budget too small for one batch is refused at creation.
     with pytest.raises(RuntimeError):
         bdcudatag.Server([(w, h, fams)], device_budget=1 << 20)

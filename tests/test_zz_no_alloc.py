@@ -33,7 +33,7 @@ def reference_stats(img, stride_img):
 def test_noalloc_matches_detector_twice():
     torch = pytest.importorskip("torch")
     lib = bdcudatag.lib()
-    frames = [scenes.render_config(2, 5, 1280, 800)[0], scenes.render_config(3, 11, 1001, 777)[0]]
+    frames = [scenes.render_scene(scenes.MIXED_1280, 5, 1280, 800)[0], scenes.render_scene(scenes.MULTI_SIZE, 11, 1001, 777)[0]]
     stream = torch.cuda.current_stream()
     for img in frames:  # two calls in a row, different sizes and contents
         h, w = img.shape
