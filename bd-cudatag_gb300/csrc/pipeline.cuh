@@ -118,7 +118,7 @@ struct LaunchConfig {
     int stats_rows = 1;        // tile rows per k_stats CTA: 1, 2 or 4
     int quad_warps = 4;        // warps (= candidates in flight) per k_fit_decode CTA: 2, 4 or 8
     int quad_ctas_per_sm = 8;  // persistent fit/decode grid = SMs * this (capped by the work)
-    int quad_split = 48;       // candidates with a bbox side above this (px) take a CTA each; 0: none
+    int quad_split = 32;       // candidates with a bbox side above this (px) take a CTA each; 0: none
     int band_cap = 2048;       // runs of a band unioned in shared memory (256..2048); more: fallback
 };
 
