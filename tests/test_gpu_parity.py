@@ -234,7 +234,7 @@ def test_caps_exceeded():
 def test_batch_matches_single_frames():
     sizes = [(640, 480), (1280, 800), (1600, 1304), (1920, 1080)] * 2
     frames, _ = scenes.render_many(scenes.MULTI_SIZE, sizes, threads=8)
-    cams = [(w, h, 3 if i % 3 else 1) for i, (w, h) in enumerate(sizes)]
+    cams = [(w, h, (3, 1, 2)[i % 3]) for i, (w, h) in enumerate(sizes)]  # both, 36h11, 16h5
     batch = bdcudatag.Batch(cams)
     found, out = batch.detect(frames)
     for i, (w, h, fams) in enumerate(cams):
