@@ -448,11 +448,30 @@ int32_t bd_batch_pipeline(bd_batch* const* batches, int32_t count, const uint8_t
     }
     const int cams = batches[0] ? batches[0]->plan->frames() : 0;
     for (int i = 0; i < count; ++i) {
-        if (!batches[i] || batches[i]->plan->frames() != cams) {
-            set_error("bd_batch_pipeline: batches must be non-null with the same cameras");
+        bool same = batches[i] && batches[i]->plan->frames() == cams;
+        for (int c = 0; same && c < cams; ++c) {
+            const bdgb::PlanFrame& a = batches[i]->plan->frame(c);
+            const bdgb::PlanFrame& b0 = batches[0]->plan->frame(c);
+            same = a.width == b0.width && a.height == b0.height && a.families == b0.families;
+        }
+        for (int j = 0; same && j < i; ++j) same = batches[j] != batches[i];
+        if (!same) {
+            set_error("bd_batch_pipeline: batches must be distinct, non-null, with the same cameras");
             return BD_ERROR_INVALID_ARGUMENT;
         }
     }
+    for (int k = 0; k < sets; ++k) {
+        const int bad = batch_check(batches[0], frames + static_cast<size_t>(k) * cams, strides);
+        if (bad != BD_OK) return bad;
+    }
+    // Each batch is used by this call alone while it runs; the mutexes are
+    // taken in address order so concurrent callers cannot deadlock.
+    std::vector<std::mutex*> order;
+    for (int i = 0; i < count; ++i) order.push_back(&batches[i]->plan->mutex());
+    std::sort(order.begin(), order.end());
+    std::vector<std::unique_lock<std::mutex>> locks;
+    locks.reserve(count);
+    for (std::mutex* m : order) locks.emplace_back(*m);
     std::vector<bool> busy(count, false);
     std::vector<int> step_of(count, -1);
     std::vector<Clock::time_point> issued(count);
