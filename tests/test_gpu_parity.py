@@ -315,3 +315,25 @@ def test_launch_shapes_and_autotune_keep_results():
         for fam in (0, 1):
             n, d = bdcudatag.Detector(fam, w, h).detect(frames[i])
             assert found[i, fam] == n and out[i, fam, :n].tobytes() == d.tobytes()
+
+
+def test_pipeline_runner_checks_and_results():
+    torch = pytest.importorskip("torch")
+    img, _ = scenes.render_scene(scenes.MIXED_1280, 2, 1280, 800)
+    frame = torch.from_numpy(img).cuda()
+    a = bdcudatag.Batch([(1280, 800, 3)])
+    b = bdcudatag.Batch([(1280, 800, 3)])
+    other = bdcudatag.Batch([(640, 480, 3)])
+    with pytest.raises(RuntimeError):
+        bdcudatag.pipeline([a, other], [[frame]], [1280], 2, True)  # different cameras
+    with pytest.raises(RuntimeError):
+        bdcudatag.pipeline([a, a], [[frame]], [1280], 2, True)  # the same batch twice
+    with pytest.raises(RuntimeError):
+        bdcudatag.pipeline([a, b], [[frame]], [1000], 2, True)  # stride below the width
+    wall, lat = bdcudatag.pipeline([a, b], [[frame]], [1280], 5, True)
+    assert wall > 0 and len(lat) == 5 and all(v > 0 for v in lat)
+    found, out = b.wait()  # the last batch on b holds the frame's results
+    for fam in (0, 1):
+        n, want = oracle.Frame(img, fam).detections()
+        assert found[0, fam] == n
+        same_records(out[0, fam, :n], want)
