@@ -339,6 +339,7 @@ int64_t bd_server_submit(bd_server* s, int32_t camera, const uint8_t* gray, int3
         bdgb::set_last_error("bd_server_submit: camera queue is full");
         return BD_ERROR_OUT_OF_MEMORY;
     }
+    s->outstanding[camera] += 1;  // reserved before the lock is released for a copy
     Request r;
     r.camera = camera;
     r.arrival = arrival;
@@ -359,7 +360,6 @@ int64_t bd_server_submit(bd_server* s, int32_t camera, const uint8_t* gray, int3
         r.stride = cam.width;
     }
     const int64_t ticket = s->next_ticket++;
-    s->outstanding[camera] += 1;
     s->requests.emplace(ticket, std::move(r));
     s->pending[camera].push_back(ticket);
     ++s->submitted;
