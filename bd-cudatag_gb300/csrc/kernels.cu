@@ -1055,8 +1055,9 @@ __device__ bool hull_to_quad_warp(const uint32_t* hull, int count, float quad[4]
     float vx = lane < count ? static_cast<float>(hull[lane] & 0xffffu) : 0.0f;
     float vy = lane < count ? static_cast<float>(hull[lane] >> 16) : 0.0f;
     while (count > 4) {
-        const int prev = (lane + count - 1) % count;
-        const int next = (lane + 1) % count;
+        // Cyclic neighbours (lanes >= count compute garbage that is unused).
+        const int prev = lane == 0 ? count - 1 : lane - 1;
+        const int next = lane + 1 >= count ? 0 : lane + 1;
         const float pvx = __shfl_sync(kFull, vx, prev), pvy = __shfl_sync(kFull, vy, prev);
         const float nvx = __shfl_sync(kFull, vx, next), nvy = __shfl_sync(kFull, vy, next);
         float area = FLT_MAX;
@@ -1245,8 +1246,9 @@ __device__ void fit_edges_warp(const float (*q)[2], const uint8_t* __restrict__ 
     }
     const int seg = __reduce_max_sync(kFull, static_cast<unsigned>(my_samples)) <= 8 ? 8 : 16;
     float* mags = s_mags + lane * kMaxProbes;
-    for (int base = 0; base < 4; base += 32 / seg) {
-        const int edge = base + lane / seg;
+    const int seg_shift = seg == 8 ? 3 : 4;
+    for (int base = 0; base < 4; base += 32 >> seg_shift) {
+        const int edge = base + (lane >> seg_shift);
         const int sample = lane & (seg - 1);
         const int bi = (edge + 1) & 3;
         const float ax = q[edge][0], ay = q[edge][1];
@@ -1570,6 +1572,10 @@ struct VariantResult {
     float corners[8];
 };
 
+// c / dim for a cell index c < 64 of a 6- or 8-cell grid without an
+// integer division: (c * 43) >> 8 == c / 6 for every c < 128.
+__device__ __forceinline__ int cell_row(int c, int dim) { return dim == 8 ? (c >> 3) : ((c * 43) >> 8); }
+
 // Decodes the four rotations of one quad at once (reference decode_quad
 // :1291-1436, one call per variant there): lanes 8r..8r+7 take rotation r,
 // lane 8r+u sampling cells u, u+8, ... of the dim x dim grid with the
@@ -1604,7 +1610,7 @@ __device__ int decode_rotations_warp(const uint8_t* __restrict__ gray, const Fra
     float* raw = s_raw[g];
     if (alive) {
         for (int c = u; c < cells; c += 8) {
-            const int cy = c / dim, cx = c - cy * dim;
+            const int cy = cell_row(c, dim), cx = c - cy * dim;
             const float uu = cell_uv[cx];  // (cx + 0.5f) / dim
             const float vv = cell_uv[cy];
             const float den = h[6] * uu + h[7] * vv + 1.0f;
@@ -1631,7 +1637,7 @@ __device__ int decode_rotations_warp(const uint8_t* __restrict__ gray, const Fra
     bool border_bad = false;
     if (alive) {
         for (int c = u; c < cells; c += 8) {
-            const int cy = c / dim, cx = c - cy * dim;
+            const int cy = cell_row(c, dim), cx = c - cy * dim;
             if (cx == 0 || cy == 0 || cx == dim - 1 || cy == dim - 1) {
                 border_bad = border_bad || raw[c] >= thresh;
             }
@@ -1648,7 +1654,7 @@ __device__ int decode_rotations_warp(const uint8_t* __restrict__ gray, const Fra
     if (alive) {
         float* sharp = s_sharp[g];
         for (int c = u; c < cells; c += 8) {
-            const int cy = c / dim, cx = c - cy * dim;
+            const int cy = cell_row(c, dim), cx = c - cy * dim;
             float sv = raw[c];
             if (cx >= 1 && cy >= 1 && cx <= dim - 2 && cy <= dim - 2) {
                 const float cc = raw[c];
