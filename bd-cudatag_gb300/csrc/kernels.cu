@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
                 }
             }
             const uint32_t count = static_cast<uint32_t>(rows * cols);
-            const uint32_t mean = (sum + count / 2) / count;
+            const uint32_t mean = count == 64u ? (sum + 32u) >> 6 : (sum + count / 2) / count;
             const int idx = ty * tw + tx;
             d.tile_min[idx] = static_cast<uint8_t>(mn);
             d.tile_max[idx] = static_cast<uint8_t>(mx);
@@ -1918,7 +1918,7 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
             uint32_t lp = kNone, rp = kNone;
             const int s = s0 + lane;
             if (s < kept) {
-                const int y = y0 + (kept > 1 ? (s * (rows - 1)) / (kept - 1) : 0);
+                const int y = y0 + (kept == rows ? s : (s * (rows - 1)) / (kept - 1));  // kept < rows: kept > 1
                 row_extremes(d, root, x0, x1, y, &lp, &rp);
             }
             const int count = min(32, kept - s0);
@@ -2140,7 +2140,7 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
             const int points = 2 * kept;
 
             for (int s = tid; s < kept; s += blockDim.x) {
-                const int y = y0 + (kept > 1 ? (s * (rows - 1)) / (kept - 1) : 0);
+                const int y = y0 + (kept == rows ? s : (s * (rows - 1)) / (kept - 1));  // kept < rows: kept > 1
                 row_extremes(d, root, x0, x1, y, &boundary[2 * s], &boundary[2 * s + 1]);
             }
             __syncthreads();
