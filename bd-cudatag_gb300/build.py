@@ -29,7 +29,7 @@ LIB = PKG / "libbdcudatag.so"
 SCENES_LIB = PKG / "libbdscenes.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CUDA_SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu", "refine.cu"]
+CUDA_SOURCES = ["k_front.cu", "k_quad.cu", "k_finalize.cu", "engine.cu", "noalloc.cu", "refine.cu"]
 CXX_SOURCES = ["capi.cpp", "server.cpp"]
 
 

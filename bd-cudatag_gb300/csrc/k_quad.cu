@@ -1,1006 +1,17 @@
-// sm_103a kernels of the batched AprilTag pipeline.
-//
-// One launch per stage covers every frame of a batch (see pipeline.cuh).
-// Stage map, with the reference kernels each one replaces
-// (detector/src/gpu_detector.cu):
-//   k_stats          tile min/max/mean, span+mean histograms, active extents,
-//                    and (last CTA of a frame) noise floor + Otsu + ROI rows
-//                    <- k_tile_stats :104, k_tile_histograms :140,
-//                       k_tile_reference :174, k_build_row_roi :282
-//   k_binarize_runs  3x3 pooled threshold, bit-packed binarization of the
-//                    row band, run extraction  <- k_tile_threshold :237,
-//                       k_binarize :362, k_find_runs :427
-//   k_merge          8-connected union-find of runs  <- k_merge_runs :509
-//   k_region_stats   area / bbox per root  <- k_region_stats :562
-//   k_cand_count     root flattening, tag-like filter, ordered per-band
-//                    bin ranks; the frame's last CTA computes the bin bases
-//                    and places the candidates  <- k_collect_candidates :591,
-//                    k_order_candidates :642
-//   k_fit_decode     warp per candidate: hull, four corners, per-family
-//                    edge refinement and decode  <- k_fit_quads :1081,
-//                    k_decode_quads :1438
-//   k_finalize       de-duplication, sort by id, FP64 homography
-//                    <- k_finalize :1542, host fill_homography :1739
-//
-// All FP32 arithmetic follows the reference expressions term by term and is
-// compiled with -fmad=false; transcendentals come from detmath.h.  With the
-// oracle built the same way, corners and margins match it bit for bit.
+// Quad fit and decode of the candidates: hull, four corners, edge
+// refinement, the four rotations of each quad, FP64 homography.  All FP32
+// arithmetic follows the reference expressions term by term and is compiled
+// with -fmad=false; transcendentals come from detmath.h.  With the oracle
+// built the same way, corners and margins match it bit for bit.
 
-#include <cuda_runtime.h>
-
-#include <cfloat>
-#include <climits>
-#include <algorithm>
-#include <cstdint>
-
-#include "detmath.h"
+#include "kernels_common.cuh"
+#include "kernels.cuh"
 #include "families_data.inc"
-#include "pipeline.cuh"
 
 namespace bdgb {
-namespace {
 
 __device__ const uint64_t d_codes36h11[BD_CODEWORDS_36H11_COUNT] = {BD_CODEWORDS_36H11};
 __device__ const uint64_t d_codes16h5[BD_CODEWORDS_16H5_COUNT] = {BD_CODEWORDS_16H5};
-
-constexpr unsigned kFull = 0xffffffffu;
-
-__device__ __forceinline__ int family_dim(int fam) { return fam == 0 ? 8 : 6; }
-
-__device__ __forceinline__ int frame_of_band(const BatchDesc* __restrict__ b, int band) {
-    int lo = 0, hi = b->frames - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (b->band_prefix[mid] <= band) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-__device__ __forceinline__ uint32_t lanemask_lt() {
-    return (1u << (threadIdx.x & 31)) - 1u;
-}
-
-// 4 bits, bit k = (byte k of `pixels` > t).
-__device__ __forceinline__ uint32_t white_bits4(uint32_t pixels, uint32_t t4) {
-    const uint32_t gt = __vcmpgtu4(pixels, t4);  // 0xff per byte where pixel > t
-    return (((gt >> 7) & 0x01010101u) * 0x10204080u) >> 28;
-}
-
-// ---------------------------------------------------------------------------
-// Union-find with the reference's invariant: a label only ever moves to a
-// smaller slot id, so the root of a component is its smallest run slot
-// (gpu_detector.cu:398-421).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
-    for (;;) {
-        const uint32_t p = parent[x];
-        if (p == x) return x;
-        const uint32_t gp = parent[p];
-        parent[x] = gp;
-        x = gp;
-    }
-}
-
-__device__ __forceinline__ uint32_t uf_root_readonly(const uint32_t* parent, uint32_t x) {
-    for (;;) {
-        const uint32_t p = __ldcg(parent + x);
-        if (p == x) return x;
-        x = p;
-    }
-}
-
-__device__ __forceinline__ void uf_union(uint32_t* parent, uint32_t a, uint32_t b) {
-    a = uf_find(parent, a);
-    b = uf_find(parent, b);
-    while (a != b) {
-        if (a > b) {
-            const uint32_t t = a;
-            a = b;
-            b = t;
-        }
-        const uint32_t old = atomicMin(&parent[b], a);
-        if (old == a) break;
-        b = uf_find(parent, old);
-    }
-}
-
-// ===========================================================================
-// 1. Tile statistics, histograms, active extents; the last CTA of a frame
-//    computes the frame references and the ROI row count.
-// ===========================================================================
-__global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
-                                               const FrameIO* __restrict__ io) {
-    __shared__ uint32_t s_span[256];
-    __shared__ uint32_t s_mean[64];
-    __shared__ int s_lo, s_hi, s_last;
-    __shared__ float s_wb[64], s_sb[64], s_tot[2];
-    __shared__ float s_best_val[2];
-    __shared__ int s_best_idx[2];
-
-    const int tid = threadIdx.x;
-    // CTA c of a frame covers tile rows [c * R, c * R + R), R = stats_rows.
-    int fi = 0;
-    {
-        int lo = 0, hi = b->frames - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (b->stats_prefix[mid] <= static_cast<int>(blockIdx.x)) lo = mid; else hi = mid - 1;
-        }
-        fi = lo;
-    }
-    if (!io[fi].gray) return;  // slot not used in this launch
-    const FrameDesc& d = b->f[fi];
-    const int R = b->stats_rows;
-    const int cta = blockIdx.x - b->stats_prefix[fi];
-    const int n_ctas = b->stats_prefix[fi + 1] - b->stats_prefix[fi];
-    FrameState* st = d.state;
-
-    s_span[tid] = 0;
-    if (tid < 64) s_mean[tid] = 0;
-
-    const uint8_t* gray = io[fi].gray;
-    const int64_t stride = io[fi].stride;
-    const int W = d.width, H = d.height, tw = d.tile_w;
-    const bool vec = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 7u) == 0;
-    const int ty_end = min((cta + 1) * R, d.tile_h);
-    for (int ty = cta * R; ty < ty_end; ++ty) {
-        if (tid == 0) {
-            s_lo = INT_MAX;
-            s_hi = -1;
-        }
-        __syncthreads();
-        const int y0 = ty * kTile;
-        const int rows = min(kTile, H - y0);
-        int lo = INT_MAX, hi = -1;
-        for (int tx = tid; tx < tw; tx += blockDim.x) {
-            const int x0 = tx * kTile;
-            const int cols = min(kTile, W - x0);
-            const uint8_t* p = gray + static_cast<int64_t>(y0) * stride + x0;
-            uint32_t mn, mx, sum = 0;
-            if (vec && cols == kTile) {
-                uint32_t vmin = 0xffffffffu, vmax = 0u;
-                for (int r = 0; r < rows; ++r) {
-                    const uint2 v = *reinterpret_cast<const uint2*>(p + r * stride);
-                    vmin = __vminu4(vmin, __vminu4(v.x, v.y));
-                    vmax = __vmaxu4(vmax, __vmaxu4(v.x, v.y));
-                    sum = __dp4a(v.x, 0x01010101u, sum);
-                    sum = __dp4a(v.y, 0x01010101u, sum);
-                }
-                mn = min(min(vmin & 0xffu, (vmin >> 8) & 0xffu), min((vmin >> 16) & 0xffu, vmin >> 24));
-                mx = max(max(vmax & 0xffu, (vmax >> 8) & 0xffu), max((vmax >> 16) & 0xffu, vmax >> 24));
-            } else {
-                mn = 255u;
-                mx = 0u;
-                for (int r = 0; r < rows; ++r) {
-                    for (int c = 0; c < cols; ++c) {
-                        const uint32_t v = p[r * stride + c];
-                        mn = min(mn, v);
-                        mx = max(mx, v);
-                        sum += v;
-                    }
-                }
-            }
-            const uint32_t count = static_cast<uint32_t>(rows * cols);
-            const uint32_t mean = count == 64u ? (sum + 32u) >> 6 : (sum + count / 2) / count;
-            const int idx = ty * tw + tx;
-            d.tile_min[idx] = static_cast<uint8_t>(mn);
-            d.tile_max[idx] = static_cast<uint8_t>(mx);
-            atomicAdd(&s_span[(mx - mn) & 0xffu], 1u);
-            atomicAdd(&s_mean[mean >> 2], 1u);
-            if (static_cast<int>(mx - mn) >= kMinTileContrast) {
-                lo = min(lo, tx);
-                hi = max(hi, tx);
-            }
-        }
-        lo = __reduce_min_sync(kFull, lo);
-        hi = __reduce_max_sync(kFull, hi);
-        if ((tid & 31) == 0 && hi >= 0) {
-            atomicMin(&s_lo, lo);
-            atomicMax(&s_hi, hi);
-        }
-        __syncthreads();
-        if (tid == 0) {
-            d.row_lo[ty] = s_hi >= 0 ? s_lo : -1;
-            d.row_hi[ty] = s_hi;
-            if (s_hi >= 0) {
-                atomicMax(&st->top_enc, static_cast<uint32_t>(d.tile_h - ty));
-                atomicMax(&st->bottom_enc, static_cast<uint32_t>(ty + 1));
-            }
-        }
-        __syncthreads();
-    }
-    if (s_span[tid]) atomicAdd(&st->span_hist[tid], s_span[tid]);
-    if (tid < 64 && s_mean[tid]) atomicAdd(&st->mean_hist[tid], s_mean[tid]);
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&st->done_stats, 1u) == static_cast<uint32_t>(n_ctas - 1);
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-
-    // --- frame references (reference k_tile_reference :174-230) ---
-    const int lane = tid & 31;
-    if (tid < 32) {
-        // Lower quartile of the span histogram: first bin whose cumulative
-        // count exceeds total / 4.
-        uint32_t v[8];
-        uint32_t local = 0;
-        for (int k = 0; k < 8; ++k) {
-            v[k] = __ldcg(&st->span_hist[lane * 8 + k]);
-            local += v[k];
-        }
-        uint32_t incl = local;
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t n = __shfl_up_sync(kFull, incl, off);
-            if (lane >= off) incl += n;
-        }
-        const uint32_t total = __shfl_sync(kFull, incl, 31);
-        uint32_t span = 0;
-        if (total > 0) {
-            const uint32_t target = total / 4;
-            uint32_t seen = incl - local;
-            int hit = -1;
-            for (int k = 0; k < 8; ++k) {
-                seen += v[k];
-                if (hit < 0 && seen > target) hit = lane * 8 + k;
-            }
-            const unsigned any = __ballot_sync(kFull, hit >= 0);
-            span = static_cast<uint32_t>(__shfl_sync(kFull, hit, __ffs(any) - 1));
-        }
-        if (lane == 0) st->ref[0] = span;
-    } else if (tid == 32) {
-        // Otsu prefix sums, sequential so every float sum is rounded in the
-        // reference's order.
-        float total = 0.0f, sum = 0.0f;
-        for (int i = 0; i < 64; ++i) {
-            const float m = static_cast<float>(__ldcg(&st->mean_hist[i]));
-            total += m;
-            sum += static_cast<float>(i) * m;
-            s_wb[i] = total;
-            s_sb[i] = sum;
-        }
-        s_tot[0] = total;
-        s_tot[1] = sum;
-    }
-    __syncthreads();
-    if (tid < 64) {
-        // Between-class variance of every split; first maximum wins.
-        const float total = s_tot[0], sum = s_tot[1];
-        const float wb = s_wb[tid];
-        const float wa = total - wb;
-        float between = -2.0f;
-        if (total > 0.0f && wb > 0.0f && wa > 0.0f) {
-            const float sb = s_sb[tid];
-            const float mean_below = sb / wb;
-            const float mean_above = (sum - sb) / wa;
-            const float delta = mean_below - mean_above;
-            between = wb * wa * delta * delta;
-        }
-        int idx = tid;
-        for (int off = 16; off > 0; off >>= 1) {
-            const float ov = __shfl_down_sync(kFull, between, off);
-            const int oi = __shfl_down_sync(kFull, idx, off);
-            if (ov > between || (ov == between && oi < idx)) {
-                between = ov;
-                idx = oi;
-            }
-        }
-        if (lane == 0) {
-            s_best_val[tid >> 5] = between;
-            s_best_idx[tid >> 5] = idx;
-        }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        float best = s_best_val[0];
-        int idx = s_best_idx[0];
-        if (s_best_val[1] > best) {
-            best = s_best_val[1];
-            idx = s_best_idx[1];
-        }
-        const int otsu = best > -1.0f ? idx : 0;
-        st->ref[1] = static_cast<uint32_t>(otsu * 4 + 2);
-        // ROI tile rows: every row between the first and last contrasting
-        // tile row, one row of halo each side (reference :314-330, :2117).
-        const uint32_t te = __ldcg(&st->top_enc), be = __ldcg(&st->bottom_enc);
-        uint32_t roi = 0;
-        if (be > 0) {
-            const int top = d.tile_h - static_cast<int>(te);
-            const int bottom = static_cast<int>(be) - 1;
-            roi = static_cast<uint32_t>(min(bottom + 1, d.tile_h - 1) - max(top - 1, 0) + 1);
-        }
-        st->counts[4] = roi;
-    }
-}
-
-// ===========================================================================
-// 2. Pooled threshold, binarization of the row band, run extraction and the
-//    band-local connected components, for one band of 8 rows; warp w owns
-//    row y0 + w.
-//
-//    The runs of a band are unioned in shared memory (same-row fragments and
-//    8-connected runs of consecutive rows inside the band), and area / bbox
-//    are aggregated per band-local root with shared-memory atomics.  Global
-//    memory then receives one parent link per run (to its band-local root)
-//    and one aggregate per band-local root; k_merge only unions across band
-//    boundaries and k_region_stats folds band roots into global roots.  The
-//    local root is the band's smallest slot of the component, so every root
-//    is still the component's smallest slot id (reference invariant,
-//    gpu_detector.cu:398-421).  A band with more than `cap` runs (a launch
-//    shape, 256..2048) is cut into row segments of at most `cap` runs,
-//    labelled one after another, and k_merge also joins each segment's
-//    first row to the row above; only a single row longer than `cap` sends
-//    the band back to one root per run and full merging in k_merge.
-// ===========================================================================
-constexpr int kMaxBandCap = 2048;
-// Dynamic shared memory of k_binarize_runs: six arrays of `cap` run
-// entries, the band's bit rows (kTile rows of `words` words), then the row
-// (byte) of each run entry.
-__host__ __device__ constexpr size_t band_smem_bytes(int cap, int words) {
-    return (6 * static_cast<size_t>(cap) + kTile * static_cast<size_t>(words)) * sizeof(uint32_t) +
-           static_cast<size_t>(cap);
-}
-
-__device__ __forceinline__ uint32_t s_find(uint32_t* par, uint32_t x) {
-    for (;;) {
-        const uint32_t p = par[x];
-        if (p == x) return x;
-        const uint32_t gp = par[p];
-        par[x] = gp;
-        x = gp;
-    }
-}
-
-__device__ __forceinline__ void s_union(uint32_t* par, uint32_t a, uint32_t b) {
-    a = s_find(par, a);
-    b = s_find(par, b);
-    while (a != b) {
-        if (a > b) {
-            const uint32_t t = a;
-            a = b;
-            b = t;
-        }
-        const uint32_t old = atomicMin(&par[b], a);
-        if (old == a) break;
-        b = s_find(par, old);
-    }
-}
-
-__global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restrict__ b,
-                                                       const FrameIO* __restrict__ io, int cap,
-                                                       int bits_words) {
-    extern __shared__ __align__(16) uint32_t s_dyn[];
-    uint32_t* sm_run = s_dyn;
-    uint32_t* sm_par = s_dyn + cap;
-    uint32_t* sm_area = s_dyn + 2 * cap;
-    uint32_t* sm_minx = s_dyn + 3 * cap;
-    uint32_t* sm_maxx = s_dyn + 4 * cap;
-    uint32_t* sm_rows = s_dyn + 5 * cap;
-    uint32_t* sm_bits = s_dyn + 6 * cap;  // kTile rows of bits_words words
-    uint8_t* sm_row = reinterpret_cast<uint8_t*>(sm_bits + kTile * bits_words);  // cap: row of each run
-    __shared__ uint8_t s_thresh[BD_MAX_WIDTH / kTile];
-    __shared__ uint8_t s_vmin[BD_MAX_WIDTH / kTile];
-    __shared__ uint8_t s_vmax[BD_MAX_WIDTH / kTile];
-    __shared__ uint32_t s_rowtot[kTile];
-    __shared__ uint32_t s_rowoff[kTile + 1];
-    __shared__ uint32_t s_nroots;
-    __shared__ uint32_t s_segmask;
-
-    const int tid = threadIdx.x;
-    const int fi = frame_of_band(b, blockIdx.x);
-    if (!io[fi].gray) return;  // slot not used in this launch
-    const FrameDesc& d = b->f[fi];
-    const int ty = blockIdx.x - b->band_prefix[fi];
-    FrameState* st = d.state;
-    const int W = d.width, H = d.height, tw = d.tile_w, th = d.tile_h, words = d.words;
-    const int y0 = ty * kTile;
-    const int rows = min(kTile, H - y0);
-    const uint32_t row_cap = static_cast<uint32_t>(d.row_cap);
-    const uint32_t band_base = static_cast<uint32_t>(y0) * row_cap;
-
-    const int top = th - static_cast<int>(st->top_enc);
-    const int bottom = static_cast<int>(st->bottom_enc) - 1;
-    const bool on = bottom >= 0 && ty >= top - 1 && ty <= bottom + 1;
-    if (!on) {
-        for (int i = tid; i < rows * words; i += blockDim.x) {
-            d.bits[static_cast<int64_t>(y0 + i / words) * words + i % words] = 0xffffffffu;
-        }
-        if (tid < rows) d.row_count[y0 + tid] = 0;
-        if (tid == 0) {
-            d.lroot_count[ty] = 0;
-            d.band_mode[ty] = 0;
-        }
-        return;
-    }
-
-    // Row band: contrasting tiles +- 4, or the whole row (reference :345-355).
-    const int lo = d.row_lo[ty], hi = d.row_hi[ty];
-    const int start = lo < 0 ? 0 : max(0, lo - 4);
-    const int end = lo < 0 ? tw - 1 : min(tw - 1, hi + 4);
-    const int wx_lo = start >> 2;
-    const int wx_hi = end >> 2;
-
-    // Pooled thresholds (reference k_tile_threshold :237-270).
-    const uint32_t ref0 = st->ref[0], ref1 = st->ref[1];
-    const int floor_contrast = max(kMinTileContrast, static_cast<int>((ref0 * 3) / 2));
-    const int t_end = min(4 * wx_hi + 3, tw - 1);
-    // The 3x3 window min/max, separably: columns over the three tile rows
-    // (coalesced loads into shared memory), then three columns.
-    const int c_lo = max(4 * wx_lo - 1, 0), c_hi = min(t_end + 1, tw - 1);
-    for (int xx = c_lo + tid; xx <= c_hi; xx += blockDim.x) {
-        int mn = 255, mx = 0;
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int yy = ty + dy;
-            if (yy < 0 || yy >= th) continue;
-            mn = min(mn, static_cast<int>(d.tile_min[yy * tw + xx]));
-            mx = max(mx, static_cast<int>(d.tile_max[yy * tw + xx]));
-        }
-        s_vmin[xx] = static_cast<uint8_t>(mn);
-        s_vmax[xx] = static_cast<uint8_t>(mx);
-    }
-    __syncthreads();
-    for (int t = 4 * wx_lo + tid; t <= t_end; t += blockDim.x) {
-        int mn = 255, mx = 0;
-        for (int dx = -1; dx <= 1; ++dx) {
-            const int xx = t + dx;
-            if (xx < 0 || xx >= tw) continue;
-            mn = min(mn, static_cast<int>(s_vmin[xx]));
-            mx = max(mx, static_cast<int>(s_vmax[xx]));
-        }
-        int thr = static_cast<int>(ref1);
-        if (mx - mn >= floor_contrast) thr = (mn + mx + 1) >> 1;
-        s_thresh[t] = static_cast<uint8_t>(thr);
-    }
-    if (tid < kTile) s_rowtot[tid] = 0;
-    __syncthreads();
-
-    const int w = tid >> 5, lane = tid & 31;
-    const uint8_t* gray = io[fi].gray;
-    const int64_t stride = io[fi].stride;
-    const bool vec = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 15u) == 0;
-    const int per = (words + 31) >> 5;
-    const int c0 = lane * per;
-    const int c1 = min(c0 + per, words);
-    uint32_t first_index = 0;  // exclusive prefix of this lane's fragments in its row
-    if (w < rows) {
-        const int y = y0 + w;
-        const uint8_t* row = gray + static_cast<int64_t>(y) * stride;
-        for (int wx = lane; wx < words; wx += 32) {
-            uint32_t m = 0xffffffffu;
-            if (wx >= wx_lo && wx <= wx_hi) {
-                const int x = wx << 5;
-                if (vec && x + 32 <= W) {
-                    const uint4 a = *reinterpret_cast<const uint4*>(row + x);
-                    const uint4 c = *reinterpret_cast<const uint4*>(row + x + 16);
-                    const int t0 = x >> 3;
-                    const uint32_t q0 = s_thresh[t0] * 0x01010101u, q1 = s_thresh[t0 + 1] * 0x01010101u;
-                    const uint32_t q2 = s_thresh[t0 + 2] * 0x01010101u, q3 = s_thresh[t0 + 3] * 0x01010101u;
-                    m = white_bits4(a.x, q0) | (white_bits4(a.y, q0) << 4) |
-                        (white_bits4(a.z, q1) << 8) | (white_bits4(a.w, q1) << 12) |
-                        (white_bits4(c.x, q2) << 16) | (white_bits4(c.y, q2) << 20) |
-                        (white_bits4(c.z, q3) << 24) | (white_bits4(c.w, q3) << 28);
-                } else {
-                    m = 0u;
-                    for (int k = 0; k < 32; ++k) {
-                        const int xx = x + k;
-                        const bool white = xx >= W || row[xx] > s_thresh[xx >> 3];
-                        m |= (white ? 1u : 0u) << k;
-                    }
-                }
-            }
-            d.bits[static_cast<int64_t>(y) * words + wx] = m;
-            sm_bits[w * bits_words + wx] = m;
-        }
-        __syncwarp();
-        // Fragments per lane, then the row's prefix (reference :448-470).
-        uint32_t cnt = 0;
-        for (int c = c0; c < c1; ++c) {
-            const uint32_t m = sm_bits[w * bits_words + c];
-            cnt += __popc(~m & ((m << 1) | 1u));
-        }
-        uint32_t incl = cnt;
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t n = __shfl_up_sync(kFull, incl, off);
-            if (lane >= off) incl += n;
-        }
-        first_index = incl - cnt;
-        const uint32_t total = __shfl_sync(kFull, incl, 31);
-        if (lane == 0) {
-            const uint32_t kept = min(total, row_cap);
-            d.row_count[y] = kept;
-            s_rowtot[w] = kept;
-        }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t off = 0;
-        for (int r = 0; r < kTile; ++r) {
-            s_rowoff[r] = off;
-            off += s_rowtot[r];
-        }
-        s_rowoff[kTile] = off;
-        s_nroots = 0;
-        atomicAdd(&st->counts[2], off);
-        // Row segments that fit `cap` runs: a segment starts at row r > 0
-        // (bit r) where adding row r would exceed the cap.  A row longer
-        // than the cap by itself sends the band to the fallback.
-        uint32_t mask = 0, cum = 0;
-        bool fits = true;
-        for (int r = 0; r < kTile; ++r) {
-            const uint32_t n = s_rowtot[r];
-            if (n > static_cast<uint32_t>(cap)) fits = false;
-            if (cum > 0 && cum + n > static_cast<uint32_t>(cap)) {
-                mask |= 1u << r;
-                cum = 0;
-            }
-            cum += n;
-        }
-        s_segmask = fits ? mask : kNone;
-    }
-    __syncthreads();
-    const uint32_t band_total = s_rowoff[kTile];
-    const uint32_t segmask = s_segmask;
-    const bool fallback = segmask == kNone;
-    const bool single = segmask == 0u;  // the whole band fits: runs go straight to shared memory
-
-    // Emit the runs (reference :472-503).
-    if (w < rows) {
-        const int y = y0 + w;
-        const uint32_t slot_base = static_cast<uint32_t>(y) * row_cap;
-        uint32_t index = first_index;
-        for (int c = c0; c < c1; ++c) {
-            const uint32_t m = sm_bits[w * bits_words + c];
-            uint32_t starts = ~m & ((m << 1) | 1u);
-            const int last = min(31, W - 1 - (c << 5));
-            while (starts) {
-                const int s = __ffs(starts) - 1;
-                starts &= starts - 1u;
-                const int x0 = (c << 5) + s;
-                if (x0 < W && index < row_cap) {
-                    const int next_white = __ffs(m >> s);
-                    int e = next_white ? (s + next_white - 2) : last;
-                    e = min(e, last);
-                    const int x1 = (c << 5) + e;
-                    const uint32_t id = slot_base + index;
-                    const uint32_t packed = (static_cast<uint32_t>(x0) & 0xffffu) | (static_cast<uint32_t>(x1) << 16);
-                    d.runs[id] = packed;
-                    if (single) {
-                        const uint32_t li = s_rowoff[w] + index;
-                        sm_run[li] = packed;
-                        sm_par[li] = li;
-                        sm_row[li] = static_cast<uint8_t>(w);
-                    } else if (fallback) {
-                        // Every run is its own band root.
-                        d.parent[id] = id;
-                        d.area[id] = static_cast<uint32_t>(x1 - x0 + 1);
-                        reinterpret_cast<uint4*>(d.bbox)[id] = make_uint4(x0, y, x1, y);
-                        d.lroots[band_base + s_rowoff[w] + index] = id;
-                    }
-                }
-                ++index;
-            }
-        }
-    }
-    if (fallback) {
-        if (tid == 0) {
-            d.lroot_count[ty] = band_total;
-            d.band_mode[ty] = 1;
-        }
-        return;
-    }
-    __syncthreads();
-
-    // Band-local components, one row segment at a time (one segment when the
-    // band fits).  Local index i of a segment = band index seg_off + i.
-    for (int r0 = 0; r0 < kTile;) {
-        int r1 = r0 + 1;
-        while (r1 < kTile && !((segmask >> r1) & 1u)) ++r1;
-        const uint32_t seg_off = s_rowoff[r0];
-        const uint32_t seg_n = s_rowoff[r1] - seg_off;
-        for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
-            if (!single) {
-                int row = 0;
-                while (row + 1 < kTile && s_rowoff[row + 1] <= seg_off + i) ++row;
-                sm_run[i] = d.runs[static_cast<int64_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row])];
-                sm_par[i] = i;
-                sm_row[i] = static_cast<uint8_t>(row);
-            }
-            sm_area[i] = 0u;
-            sm_minx[i] = 0xffffffffu;
-            sm_maxx[i] = 0u;
-            sm_rows[i] = 0u;
-        }
-        __syncthreads();
-
-        // Unions inside the segment (the reference's k_merge_runs rules).
-        if (w >= r0 && w < r1 && w < rows) {
-            const uint32_t n = s_rowtot[w];
-            const uint32_t base = s_rowoff[w] - seg_off;
-            const uint32_t prev_n = w > r0 ? s_rowtot[w - 1] : 0u;
-            const uint32_t pbase = w > r0 ? s_rowoff[w - 1] - seg_off : 0u;
-            for (uint32_t i = lane; i < n; i += 32) {
-                const uint32_t run = sm_run[base + i];
-                const int x0 = static_cast<int>(run & 0xffffu);
-                const int x1 = static_cast<int>(run >> 16);
-                // Row 0 of the frame is never merged, not even its word-split
-                // fragments (reference k_merge_runs :514 returns for y <= 0).
-                if (i > 0 && y0 + w > 0) {
-                    const int px1 = static_cast<int>(sm_run[base + i - 1] >> 16);
-                    if (px1 + 1 >= x0) s_union(sm_par, base + i, base + i - 1);
-                }
-                if (prev_n == 0) continue;
-                int lo2 = 0, hi2 = static_cast<int>(prev_n) - 1, first = static_cast<int>(prev_n);
-                while (lo2 <= hi2) {
-                    const int mid = (lo2 + hi2) >> 1;
-                    if (static_cast<int>(sm_run[pbase + mid] >> 16) >= x0 - 1) {
-                        first = mid;
-                        hi2 = mid - 1;
-                    } else {
-                        lo2 = mid + 1;
-                    }
-                }
-                for (int k = first; k < static_cast<int>(prev_n); ++k) {
-                    const int px0 = static_cast<int>(sm_run[pbase + k] & 0xffffu);
-                    if (px0 > x1 + 1) break;
-                    s_union(sm_par, base + i, pbase + k);
-                }
-            }
-        }
-        __syncthreads();
-
-        // Flatten the forest by pointer jumping (parents have smaller
-        // indices, so every value written is an ancestor): log-depth rounds
-        // instead of each run walking its whole chain.
-        for (;;) {
-            int changed = 0;
-            for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
-                const uint32_t p = sm_par[i];
-                const uint32_t gp = sm_par[p];
-                if (gp != p) {
-                    sm_par[i] = gp;
-                    changed = 1;
-                }
-            }
-            if (!__syncthreads_or(changed)) break;
-        }
-
-        // Segment roots (its smallest slot) and their area / bbox.
-        for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
-            const uint32_t r = sm_par[i];
-            const int row = sm_row[i];
-            const uint32_t run = sm_run[i];
-            const uint32_t x0 = run & 0xffffu, x1 = run >> 16;
-            atomicAdd(&sm_area[r], x1 - x0 + 1);
-            atomicMin(&sm_minx[r], x0);
-            atomicMax(&sm_maxx[r], x1);
-            atomicOr(&sm_rows[r], 1u << row);
-            // parent link = the local root's slot
-            const int rrow = sm_row[r];
-            const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row]);
-            const uint32_t rslot = static_cast<uint32_t>(y0 + rrow) * row_cap + (seg_off + r - s_rowoff[rrow]);
-            d.parent[slot] = rslot;
-        }
-        __syncthreads();
-        for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
-            if (sm_par[i] != i) continue;
-            const int row = sm_row[i];
-            const uint32_t slot = static_cast<uint32_t>(y0 + row) * row_cap + (seg_off + i - s_rowoff[row]);
-            const uint32_t rm = sm_rows[i];
-            d.area[slot] = sm_area[i];
-            reinterpret_cast<uint4*>(d.bbox)[slot] =
-                make_uint4(sm_minx[i], static_cast<uint32_t>(y0 + __ffs(rm) - 1), sm_maxx[i],
-                           static_cast<uint32_t>(y0 + 31 - __clz(rm)));
-            d.lroots[band_base + atomicAdd(&s_nroots, 1u)] = slot;
-        }
-        __syncthreads();
-        r0 = r1;
-    }
-    if (tid == 0) {
-        d.lroot_count[ty] = s_nroots;
-        d.band_mode[ty] = segmask;  // bit r: row r starts a segment (k_merge joins it to row r - 1)
-    }
-}
-
-// ===========================================================================
-// 3. Unions across band boundaries: the first row of a band against the last
-//    row of the band above; every row of a fallback band (the reference's
-//    k_merge_runs :509-557 rules).
-// ===========================================================================
-__device__ __forceinline__ void merge_run_with_row_above(uint32_t* parent, const uint32_t* cur,
-                                                         const uint32_t* prev, int i, int prev_n,
-                                                         uint32_t cur_base, uint32_t prev_base,
-                                                         bool same_row) {
-    const uint32_t run = cur[i];
-    const int x0 = static_cast<int>(run & 0xffffu);
-    const int x1 = static_cast<int>(run >> 16);
-    if (same_row && i > 0) {
-        const int px1 = static_cast<int>(cur[i - 1] >> 16);
-        if (px1 + 1 >= x0) uf_union(parent, cur_base + i, cur_base + i - 1);
-    }
-    if (prev_n == 0) return;
-    int lo = 0, hi = prev_n - 1, first = prev_n;
-    while (lo <= hi) {
-        const int mid = (lo + hi) >> 1;
-        if (static_cast<int>(prev[mid] >> 16) >= x0 - 1) {
-            first = mid;
-            hi = mid - 1;
-        } else {
-            lo = mid + 1;
-        }
-    }
-    for (int k = first; k < prev_n; ++k) {
-        const int px0 = static_cast<int>(prev[k] & 0xffffu);
-        if (px0 > x1 + 1) break;
-        uf_union(parent, cur_base + i, prev_base + k);
-    }
-}
-
-__global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b,
-                                               const FrameIO* __restrict__ io, int row_cap_max) {
-    const int fi = frame_of_band(b, blockIdx.x);
-    if (!io[fi].gray) return;  // slot not used in this launch
-    const FrameDesc& d = b->f[fi];
-    const int ty = blockIdx.x - b->band_prefix[fi];
-    const int row_cap = d.row_cap;
-    uint32_t* parent = d.parent;
-    const uint32_t mode = d.band_mode[ty];
-    if (!(mode & 1u)) {
-        // Band-local unions are done: the first row of the band, and the
-        // first row of every further segment (bit r of the mode), meet the
-        // row above.  Both rows are staged in shared memory (the searches
-        // run there); their runs are spread over the whole CTA.
-        extern __shared__ __align__(16) uint32_t s_dyn[];
-        uint32_t* s_prev = s_dyn;
-        uint32_t* s_cur = s_dyn + row_cap_max;
-        for (uint32_t starts = mode | 1u; starts; starts &= starts - 1u) {
-            const int y = ty * kTile + __ffs(starts) - 1;
-            if (y <= 0 || y >= d.height) continue;  // uniform over the CTA
-            const int n = static_cast<int>(d.row_count[y]);
-            const int prev_n = static_cast<int>(d.row_count[y - 1]);
-            const uint32_t* cur = d.runs + static_cast<int64_t>(y) * row_cap;
-            const uint32_t* prev = d.runs + static_cast<int64_t>(y - 1) * row_cap;
-            for (int i = threadIdx.x; i < prev_n; i += blockDim.x) s_prev[i] = prev[i];
-            for (int i = threadIdx.x; i < n; i += blockDim.x) s_cur[i] = cur[i];
-            __syncthreads();
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                merge_run_with_row_above(parent, s_cur, s_prev, i, prev_n,
-                                         static_cast<uint32_t>(y * row_cap),
-                                         static_cast<uint32_t>((y - 1) * row_cap), false);
-            }
-            __syncthreads();  // the next pair reuses the buffers
-        }
-        return;
-    }
-    // Fallback band: every row, one warp per row.
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int y = ty * kTile + w;
-    if (y <= 0 || y >= d.height) return;
-    const int n = static_cast<int>(d.row_count[y]);
-    const int prev_n = static_cast<int>(d.row_count[y - 1]);
-    const uint32_t* cur = d.runs + static_cast<int64_t>(y) * row_cap;
-    const uint32_t* prev = d.runs + static_cast<int64_t>(y - 1) * row_cap;
-    for (int i = lane; i < n; i += 32) {
-        merge_run_with_row_above(parent, cur, prev, i, prev_n, static_cast<uint32_t>(y * row_cap),
-                                 static_cast<uint32_t>((y - 1) * row_cap), true);
-    }
-}
-
-// ===========================================================================
-// 4. Area and bounding box per global root: each band root adds its
-//    aggregate to its global root (reference k_region_stats :562-586 sums the
-//    same quantities run by run).
-// ===========================================================================
-__global__ void __launch_bounds__(256) k_region_stats(const BatchDesc* __restrict__ b,
-                                                      const FrameIO* __restrict__ io) {
-    const int fi = frame_of_band(b, blockIdx.x);
-    if (!io[fi].gray) return;  // slot not used in this launch
-    const FrameDesc& d = b->f[fi];
-    const int ty = blockIdx.x - b->band_prefix[fi];
-    const uint32_t n = d.lroot_count[ty];
-    const uint32_t* list = d.lroots + static_cast<int64_t>(ty) * kTile * d.row_cap;
-    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-        const uint32_t s = list[k];
-        const uint32_t g = uf_find(d.parent, s);
-        if (g == s) continue;
-        d.parent[s] = g;  // later label walks take two hops
-        const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[s];
-        atomicAdd(&d.area[g], d.area[s]);
-        atomicMin(&d.bbox[g * 4 + 0], bb.x);
-        atomicMin(&d.bbox[g * 4 + 1], bb.y);
-        atomicMax(&d.bbox[g * 4 + 2], bb.z);
-        atomicMax(&d.bbox[g * 4 + 3], bb.w);
-    }
-}
-
-// ===========================================================================
-// 5. Root labels, the tag-like filter and ordered ranks.  A candidate's
-//    flattened position is (area bin, band, row, slot) order, which is
-//    ascending root id inside a bin; the reference orders a bin by atomicAdd
-//    arrival (k_collect_candidates :591-638).
-// ===========================================================================
-__device__ __forceinline__ int candidate_bin(const FrameDesc& d, uint32_t idx) {
-    const int a = static_cast<int>(d.area[idx]);
-    if (a < d.min_cluster_pixels) return -1;
-    const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[idx];
-    const int x0 = static_cast<int>(bb.x), y0 = static_cast<int>(bb.y);
-    const int x1 = static_cast<int>(bb.z), y1 = static_cast<int>(bb.w);
-    const int bw = x1 - x0 + 1;
-    const int bh = y1 - y0 + 1;
-    if (bw < d.min_tag_pixels || bh < d.min_tag_pixels) return -1;
-    if (x0 <= 0 || y0 <= 0 || x1 >= d.width - 1 || y1 >= d.height - 1) return -1;
-    if (bw > 6 * bh || bh > 6 * bw) return -1;
-    const float fill = static_cast<float>(a) / static_cast<float>(bw * bh);
-    if (fill < 0.18f || fill > 0.95f) return -1;
-    const int log2_area = 31 - __clz(static_cast<uint32_t>(a));
-    return 63 - min(log2_area, 63);
-}
-
-__device__ __forceinline__ uint32_t band_slot(const uint32_t* rowoff, int y0, uint32_t row_cap,
-                                              uint32_t i) {
-    int row = 0;
-    while (row + 1 < kTile && rowoff[row + 1] <= i) ++row;
-    return static_cast<uint32_t>(y0 + row) * row_cap + (i - rowoff[row]);
-}
-
-// One CTA per band, 256 runs at a time in slot order: root labels, the
-// tag-like filter, and each candidate's rank among the band's candidates
-// of its area bin.
-__global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict__ b,
-                                                    const FrameIO* __restrict__ io) {
-    __shared__ uint32_t s_rowoff[kTile + 1];
-    __shared__ uint32_t s_wbin[8][64];
-    __shared__ uint32_t s_run[64];
-    __shared__ uint32_t s_chunk[4][64];
-    __shared__ uint32_t s_total[64];
-    __shared__ uint32_t s_base[64];
-    __shared__ uint32_t s_cprefix[kMaxBandsPerFrame + 1];  // candidates before each band
-    __shared__ uint32_t s_warp_sum[8];
-    __shared__ uint32_t s_ncand, s_limit;
-    __shared__ int s_last;
-
-    const int tid = threadIdx.x;
-    const int fi = frame_of_band(b, blockIdx.x);
-    if (!io[fi].gray) return;  // slot not used in this launch
-    const FrameDesc& d = b->f[fi];
-    const int ty = blockIdx.x - b->band_prefix[fi];
-    FrameState* st = d.state;
-    const int y0 = ty * kTile;
-    const uint32_t row_cap = static_cast<uint32_t>(d.row_cap);
-    if (tid == 0) {
-        uint32_t off = 0;
-        for (int r = 0; r < kTile; ++r) {
-            s_rowoff[r] = off;
-            off += y0 + r < d.height ? d.row_count[y0 + r] : 0u;
-        }
-        s_rowoff[kTile] = off;
-    }
-    if (tid < 64) s_run[tid] = 0;
-    if (tid == 0) s_ncand = 0;
-    __syncthreads();
-    const uint32_t total = s_rowoff[kTile];
-    const int w = tid >> 5, lane = tid & 31;
-    // The band's candidate roots are listed in its lroots range (free since
-    // k_region_stats), for the frame's last CTA to place.
-    uint32_t* band_list = d.lroots + static_cast<int64_t>(ty) * kTile * row_cap;
-    for (uint32_t base = 0; base < total; base += blockDim.x) {
-        const uint32_t i = base + tid;
-        int bin = -1;
-        uint32_t slot = 0;
-        if (i < total) {
-            slot = band_slot(s_rowoff, y0, row_cap, i);
-            const uint32_t root = uf_root_readonly(d.parent, slot);
-            d.parent[slot] = root;
-            if (root == slot) bin = candidate_bin(d, slot);
-        }
-        const uint32_t key = bin >= 0 ? static_cast<uint32_t>(bin) : 64u + lane;
-        const uint32_t peers = __match_any_sync(kFull, key);
-        const uint32_t rank = __popc(peers & lanemask_lt());
-        s_wbin[w][lane] = 0;
-        s_wbin[w][lane + 32] = 0;
-        __syncthreads();
-        if (bin >= 0 && rank == 0) s_wbin[w][bin] = __popc(peers);
-        __syncthreads();
-        uint32_t meta = kNone;
-        if (bin >= 0) {
-            uint32_t pos = s_run[bin] + rank;
-            for (int w2 = 0; w2 < w; ++w2) pos += s_wbin[w2][bin];
-            meta = (static_cast<uint32_t>(bin) << 24) | pos;
-        }
-        __syncthreads();
-        if (tid < 64) {
-            uint32_t add = 0;
-            for (int w2 = 0; w2 < 8; ++w2) add += s_wbin[w2][tid];
-            s_run[tid] += add;
-        }
-        if (bin >= 0) {
-            d.cand_meta[slot] = meta;
-            band_list[atomicAdd(&s_ncand, 1u)] = slot;
-        }
-        __syncthreads();  // s_wbin is cleared for the next chunk
-    }
-    __syncthreads();
-    if (tid < 64) d.band_bins[ty * 64 + tid] = s_run[tid];
-    if (tid == 0) d.lroot_count[ty] = s_ncand;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&st->done_cands, 1u) == static_cast<uint32_t>(d.tile_h - 1);
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-
-    // Last band: exclusive prefix of every bin over the bands (in place).
-    // Thread (segment q, bin) sums a quarter of the bands (loads coalesced
-    // over the bins), the four segment sums are scanned per bin, and each
-    // thread rewrites its quarter from its segment's offset.
-    const int th = d.tile_h;
-    const int bin = tid & 63;
-    const int q = tid >> 6;
-    const int per = (th + 3) >> 2;
-    const int qb0 = min(th, q * per), qb1 = min(th, qb0 + per);
-    uint32_t sum = 0;
-#pragma unroll 4
-    for (int band = qb0; band < qb1; ++band) sum += __ldcg(&d.band_bins[band * 64 + bin]);
-    s_chunk[q][bin] = sum;
-    __syncthreads();
-    uint32_t carry = 0;
-    for (int q2 = 0; q2 < q; ++q2) carry += s_chunk[q2][bin];
-    if (q == 3) s_total[bin] = carry + sum;
-    for (int band = qb0; band < qb1; ++band) {
-        const uint32_t v = __ldcg(&d.band_bins[band * 64 + bin]);
-        d.band_bins[band * 64 + bin] = carry;
-        carry += v;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t pos = 0;
-        for (int bin = 0; bin < 64; ++bin) {
-            s_base[bin] = pos;
-            st->bin_base[bin] = pos;
-            pos += s_total[bin];
-        }
-        st->counts[0] = pos;
-        s_limit = min(pos, static_cast<uint32_t>(d.max_candidates));
-        st->n_candidates = s_limit;
-    }
-
-    // Placement (reference k_order_candidates :642-654): candidate j of the
-    // frame, flattened over the bands' lists, goes to bin base + earlier
-    // bands' count in its bin + its rank in the band.  Block scan of the
-    // per-band list lengths first.
-    const int chunk = (th + blockDim.x - 1) / blockDim.x;
-    const int cb0 = min(th, tid * chunk), cb1 = min(th, cb0 + chunk);
-    uint32_t own = 0;
-    for (int band = cb0; band < cb1; ++band) own += __ldcg(&d.lroot_count[band]);
-    uint32_t incl = own;
-    for (int off = 1; off < 32; off <<= 1) {
-        const uint32_t v = __shfl_up_sync(kFull, incl, off);
-        if (lane >= off) incl += v;
-    }
-    if (lane == 31) s_warp_sum[w] = incl;
-    __syncthreads();
-    uint32_t before = incl - own;
-    for (int w2 = 0; w2 < w; ++w2) before += s_warp_sum[w2];
-    for (int band = cb0; band < cb1; ++band) {
-        s_cprefix[band] = before;
-        before += __ldcg(&d.lroot_count[band]);
-    }
-    if (tid == blockDim.x - 1) s_cprefix[th] = before;
-    __syncthreads();
-    const uint32_t all = s_cprefix[th];
-    const uint32_t limit = s_limit;
-    for (uint32_t j = tid; j < all; j += blockDim.x) {
-        int lo = 0, hi = th - 1;  // last band with s_cprefix[band] <= j
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_cprefix[mid] <= j) lo = mid; else hi = mid - 1;
-        }
-        const uint32_t slot = __ldcg(&d.lroots[static_cast<int64_t>(lo) * kTile * row_cap + (j - s_cprefix[lo])]);
-        const uint32_t meta = __ldcg(&d.cand_meta[slot]);
-        const uint32_t cbin = meta >> 24;
-        const uint32_t pos = s_base[cbin] + __ldcg(&d.band_bins[lo * 64 + cbin]) + (meta & 0xffffffu);
-        if (pos < limit) d.candidates[pos] = slot;
-    }
-}
 
 // Image homography of a decoded tag's corners (reference host
 // fill_homography :1739-1774, FP64 as there).  Computed by the warp that
@@ -2295,207 +1306,7 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
     }
 }
 
-// ===========================================================================
-// 9. Finalize one (frame, family): detections in candidate order (first
-//    max_detections), de-duplication, stable sort by id, homography
-//    (reference k_finalize :1542-1601, host fill_homography :1739-1774 --
-//    FP64 here as there).
-// ===========================================================================
 
-constexpr int kFinalThreads = 256;
-
-__global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __restrict__ b) {
-    __shared__ DecodeOut s_in[kMaxDetectionsCap];
-    __shared__ DecodeOut s_out[kMaxDetectionsCap];
-    __shared__ int s_in_src[kMaxDetectionsCap], s_out_src[kMaxDetectionsCap];  // candidate index
-    __shared__ float s_cx[kMaxDetectionsCap], s_cy[kMaxDetectionsCap];
-    __shared__ uint32_t s_warp[kFinalThreads / 32];
-    __shared__ int s_count, s_kept;
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int fi = blockIdx.x >> 1;
-    const int fam = blockIdx.x & 1;
-    const FrameDesc& d = b->f[fi];
-    const FrameState* st = d.state;
-    FrameResultHeader* hdr = d.result;
-    if (fam == 0 && tid < 5) hdr->counts[tid] = st->counts[tid];
-    if (fam == 0 && tid == 5) hdr->pad = 0;
-    if (!(d.families & (1u << fam))) {
-        if (tid == 0) hdr->found[fam] = 0;
-        return;
-    }
-    const int n = static_cast<int>(st->n_candidates);
-    const int maxd = d.max_detections;
-    const DecodeOut* dec = d.decodes + static_cast<int64_t>(fam) * d.max_candidates;
-    if (tid == 0) s_count = 0;
-    __syncthreads();
-    // Ordered compaction of the decoded candidates.
-    for (int c = 0; c < n; c += kFinalThreads) {
-        const int i = c + tid;
-        const bool ok = i < n && dec[i].id >= 0;
-        const unsigned bal = __ballot_sync(kFull, ok);
-        if (lane == 0) s_warp[warp] = __popc(bal);
-        __syncthreads();
-        int before = s_count;
-        for (int w2 = 0; w2 < warp; ++w2) before += static_cast<int>(s_warp[w2]);
-        const int pos = before + __popc(bal & lanemask_lt());
-        if (ok && pos < maxd) {
-            s_in[pos] = dec[i];
-            s_in_src[pos] = i;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            int add = 0;
-            for (int w2 = 0; w2 < kFinalThreads / 32; ++w2) add += static_cast<int>(s_warp[w2]);
-            s_count = s_count + add;
-        }
-        __syncthreads();
-        if (s_count >= maxd) break;
-    }
-    const int m = min(s_count, maxd);
-    // De-duplication in arrival order, one warp.
-    if (warp == 0) {
-        int kept = 0;
-        for (int i = 0; i < m; ++i) {
-            const DecodeOut& dd = s_in[i];
-            float side = 0.0f, cx = 0.0f, cy = 0.0f;
-            for (int k = 0; k < 4; ++k) {
-                const int j = (k + 1) & 3;
-                side += bdmath::hypot(dd.corners[j * 2] - dd.corners[k * 2],
-                                      dd.corners[j * 2 + 1] - dd.corners[k * 2 + 1]);
-                cx += dd.corners[k * 2];
-                cy += dd.corners[k * 2 + 1];
-            }
-            side *= 0.25f;
-            cx *= 0.25f;
-            cy *= 0.25f;
-            const float limit = 0.35f * side;
-            int duplicate = -1;
-            for (int k0 = 0; k0 < kept && duplicate < 0; k0 += 32) {
-                const int k = k0 + lane;
-                const bool hit = k < kept && s_out[k].id == dd.id && fabsf(s_cx[k] - cx) < limit &&
-                                 fabsf(s_cy[k] - cy) < limit;
-                const unsigned bal = __ballot_sync(kFull, hit);
-                if (bal) duplicate = k0 + __ffs(bal) - 1;
-            }
-            __syncwarp();
-            if (lane == 0) {
-                if (duplicate >= 0) {
-                    if (dd.margin > s_out[duplicate].margin) {
-                        s_out[duplicate] = dd;
-                        s_out_src[duplicate] = s_in_src[i];
-                        s_cx[duplicate] = cx;
-                        s_cy[duplicate] = cy;
-                    }
-                } else if (kept < maxd) {
-                    s_out[kept] = dd;
-                    s_out_src[kept] = s_in_src[i];
-                    s_cx[kept] = cx;
-                    s_cy[kept] = cy;
-                }
-            }
-            if (duplicate < 0 && kept < maxd) ++kept;
-            __syncwarp();
-        }
-        if (lane == 0) s_kept = kept;
-    }
-    __syncthreads();
-    const int kept = s_kept;
-    bd_detection* dets = result_detections(hdr) + static_cast<int64_t>(fam) * maxd;
-    for (int i = tid; i < kept; i += kFinalThreads) {
-        const int id = s_out[i].id;
-        int rank = 0;
-        for (int j = 0; j < kept; ++j) {
-            const int oj = s_out[j].id;
-            rank += (oj < id || (oj == id && j < i)) ? 1 : 0;
-        }
-        bd_detection r;
-        r.id = id;
-        r.hamming = s_out[i].hamming;
-        r.decision_margin = s_out[i].margin;
-        for (int k = 0; k < 8; ++k) r.corners[k] = s_out[i].corners[k];
-        r.reserved = 0;
-        const float* hsrc = d.dec_h + (static_cast<int64_t>(fam) * d.max_candidates + s_out_src[i]) * 9;
-        for (int k = 0; k < 9; ++k) r.homography[k] = hsrc[k];
-        dets[rank] = r;
-    }
-    if (tid == 0) hdr->found[fam] = static_cast<uint32_t>(kept);
-}
-
-}  // namespace
-
-int prepare_pipeline() {
-    // Shared memory beyond 48 KB per block needs an opt-in, per device.
-    if (cudaFuncSetAttribute(k_binarize_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(band_smem_bytes(kMaxBandCap, BD_MAX_WIDTH / 32))) !=
-        cudaSuccess) {
-        return -1;
-    }
-    return cudaFuncSetAttribute(k_fit_decode, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(kMaxQuadWarps * sizeof(QuadSmem))) == cudaSuccess
-               ? 0
-               : -1;
-}
-
-const char* const kStageNames[kStageCount] = {
-    "stats", "binarize_runs", "merge", "region_stats", "cand_count",
-    "fit_decode_big", "fit_decode", "finalize"};
-
-void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* io, void* stream_ptr,
-                      const LaunchConfig& lc, int sm_count, const ForkJoin* fork,
-                      void* const* stage_events) {
-    cudaStream_t s = static_cast<cudaStream_t>(stream_ptr);
-    auto mark = [&](int k) {
-        if (stage_events) cudaEventRecord(static_cast<cudaEvent_t>(stage_events[k]), s);
-    };
-    const int bands = hd.total_bands;
-    int items = 0;  // candidate-family pairs at the caps
-    for (int f = 0; f < hd.frames; ++f) {
-        items += hd.f[f].max_candidates * __builtin_popcount(hd.f[f].families & 3u);
-    }
-    const int warps = lc.quad_warps;
-    const int quad_grid =
-        std::max(1, std::min((items + warps - 1) / warps, sm_count * lc.quad_ctas_per_sm));
-    mark(0);
-    k_stats<<<hd.stats_ctas, 256, 0, s>>>(dd, io);
-    mark(1);
-    int words_max = 1;
-    for (int f = 0; f < hd.frames; ++f) words_max = std::max(words_max, hd.f[f].words);
-    k_binarize_runs<<<bands, 256, band_smem_bytes(lc.band_cap, words_max), s>>>(dd, io, lc.band_cap,
-                                                                                 words_max);
-    mark(2);
-    int row_cap_max = 1;
-    for (int f = 0; f < hd.frames; ++f) row_cap_max = std::max(row_cap_max, hd.f[f].row_cap);
-    k_merge<<<bands, 256, 2 * row_cap_max * sizeof(uint32_t), s>>>(dd, io, row_cap_max);
-    mark(3);
-    k_region_stats<<<bands, 256, 0, s>>>(dd, io);
-    mark(4);
-    k_cand_count<<<bands, 256, 0, s>>>(dd, io);
-    mark(5);
-    const int split = lc.quad_split;
-    int cands = 0;
-    for (int f = 0; f < hd.frames; ++f) cands += hd.f[f].max_candidates;
-    const int big_grid = std::max(1, std::min(cands, sm_count));
-    const size_t quad_smem = warps * sizeof(QuadSmem);
-    if (split > 0 && fork && !stage_events) {
-        // Big candidates on a parallel branch (a fork/join in the graph).
-        cudaStream_t s2 = static_cast<cudaStream_t>(fork->stream);
-        cudaEventRecord(static_cast<cudaEvent_t>(fork->fork_event), s);
-        cudaStreamWaitEvent(s2, static_cast<cudaEvent_t>(fork->fork_event), 0);
-        k_fit_decode_big<<<big_grid, 256, 0, s2>>>(dd, io, split);
-        cudaEventRecord(static_cast<cudaEvent_t>(fork->join_event), s2);
-        k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io, split);
-        cudaStreamWaitEvent(s, static_cast<cudaEvent_t>(fork->join_event), 0);
-        mark(6);
-        mark(7);
-    } else {
-        if (split > 0) k_fit_decode_big<<<big_grid, 256, 0, s>>>(dd, io, split);
-        mark(6);
-        k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io, split);
-        mark(7);
-    }
-    k_finalize<<<hd.frames * 2, kFinalThreads, 0, s>>>(dd);
-    mark(8);
-}
+size_t quad_smem_per_warp() { return sizeof(QuadSmem); }
 
 }  // namespace bdgb

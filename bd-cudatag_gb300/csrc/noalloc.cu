@@ -49,7 +49,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 constexpr unsigned kFull = 0xffffffffu;
 
-// The per-frame part of k_stats (kernels.cu) with explicit buffers: one CTA
+// The per-frame part of k_stats (k_front.cu) with explicit buffers: one CTA
 // per tile row; the last CTA turns the histograms into the frame references.
 __global__ void __launch_bounds__(256) k_tile_stats_noalloc(const uint8_t* __restrict__ gray,
                                                             int W, int H, int64_t stride,

@@ -1,6 +1,6 @@
 // Shared layout of the batched detection pipeline: per-frame descriptors,
 // per-frame device state and result records.  Included by the kernels
-// (kernels.cu) and the host engine (engine.cu).
+// (k_front.cu, k_quad.cu, k_finalize.cu) and the host engine (engine.cu).
 //
 // One launch of each stage covers every frame of a batch.  A frame is cut
 // into "bands" of 8 pixel rows (one tile row); stages 1-6 run one CTA per
@@ -150,7 +150,7 @@ BDGB_HD inline size_t result_bytes(int max_detections) {
     return sizeof(FrameResultHeader) + 2 * static_cast<size_t>(max_detections) * sizeof(bd_detection);
 }
 
-// Launch sequence of one batch on one stream (kernels.cu).  `io` is a
+// Launch sequence of one batch on one stream (k_finalize.cu).  `io` is a
 // device array of FrameIO, one per frame.  With `fork` the big-candidate
 // kernel runs on fork->stream beside the warp-per-candidate kernel.  When
 // stage_events is not null (no fork then) it holds kStageCount + 1
