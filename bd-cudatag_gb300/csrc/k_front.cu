@@ -694,17 +694,48 @@ __global__ void __launch_bounds__(256) k_region_stats(const BatchDesc* __restric
     const int ty = blockIdx.x - b->band_prefix[fi];
     const uint32_t n = d.lroot_count[ty];
     const uint32_t* list = d.lroots + static_cast<int64_t>(ty) * kTile * d.row_cap;
-    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-        const uint32_t s = list[k];
-        const uint32_t g = uf_find(d.parent, s);
-        if (g == s) continue;
-        d.parent[s] = g;  // later label walks take two hops
-        const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[s];
-        atomicAdd(&d.area[g], d.area[s]);
-        atomicMin(&d.bbox[g * 4 + 0], bb.x);
-        atomicMin(&d.bbox[g * 4 + 1], bb.y);
-        atomicMax(&d.bbox[g * 4 + 2], bb.z);
-        atomicMax(&d.bbox[g * 4 + 3], bb.w);
+    const uint32_t lane = threadIdx.x & 31u;
+    // Warp-uniform sweep: lanes folding into the same global root combine
+    // their sums and extremes first (order-free: integer adds, min, max), so
+    // a component crossing many bands -- the background -- takes one set of
+    // atomics per warp instead of one per band root.
+    for (uint32_t base = threadIdx.x & ~31u; base < n; base += blockDim.x) {
+        const uint32_t k = base + lane;
+        uint32_t s = 0, g = 0;
+        bool fold = false;
+        if (k < n) {
+            s = list[k];
+            // All unions are done: walk to the root without compressing
+            // (the band root alone is relinked below).
+            g = uf_root_readonly(d.parent, s);
+            fold = g != s;
+        }
+        const unsigned want = __ballot_sync(kFull, fold);
+        if (!want) continue;
+        uint32_t area = 0, x0 = 0xffffffffu, y0 = 0xffffffffu, x1 = 0, y1 = 0;
+        if (fold) {
+            d.parent[s] = g;  // later label walks take two hops
+            const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[s];
+            area = d.area[s];
+            x0 = bb.x;
+            y0 = bb.y;
+            x1 = bb.z;
+            y1 = bb.w;
+        }
+        const unsigned peers = __match_any_sync(kFull, fold ? g : 0xffffffffu);
+        if (!fold) continue;
+        area = __reduce_add_sync(peers, area);
+        x0 = __reduce_min_sync(peers, x0);
+        y0 = __reduce_min_sync(peers, y0);
+        x1 = __reduce_max_sync(peers, x1);
+        y1 = __reduce_max_sync(peers, y1);
+        if (lane == static_cast<uint32_t>(__ffs(peers) - 1)) {
+            atomicAdd(&d.area[g], area);
+            atomicMin(&d.bbox[g * 4 + 0], x0);
+            atomicMin(&d.bbox[g * 4 + 1], y0);
+            atomicMax(&d.bbox[g * 4 + 2], x1);
+            atomicMax(&d.bbox[g * 4 + 3], y1);
+        }
     }
 }
 
