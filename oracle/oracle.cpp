@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <thread>
 #include <vector>
@@ -532,26 +533,43 @@ void row_extremes(const bdo_frame& f, uint32_t root, int bx0, int bx1, int y0, i
     }
 }
 
+// The fit below is a template on its arithmetic type.  float is the
+// restatement proper (the transcendental calls go through detmath.h, as on
+// the GPU); double is the FP64 re-fit that the FP32 corners are measured
+// against (bdo_refit64), with the C library's functions.
+inline float fm_atan2(float y, float x) { return bdmath::atan2(y, x); }
+inline double fm_atan2(double y, double x) { return std::atan2(y, x); }
+inline void fm_sincos(float a, float* s, float* c) { bdmath::sincos(a, s, c); }
+inline void fm_sincos(double a, double* s, double* c) {
+    *s = std::sin(a);
+    *c = std::cos(a);
+}
+inline float fm_hypot(float a, float b) { return bdmath::hypot(a, b); }
+inline double fm_hypot(double a, double b) { return std::hypot(a, b); }
+inline float two_pi(float) { return 6.28318530718f; }
+inline double two_pi(double) { return 6.283185307179586; }
+
 // hull_to_quad :736-831
-bool hull_to_quad(const uint32_t* hull, int count, float quad[4][2]) {
+template <typename T>
+bool hull_to_quad(const uint32_t* hull, int count, T quad[4][2]) {
     if (count < 4 || count > kMaxHullVertices) return false;
-    float vx[kMaxHullVertices];
-    float vy[kMaxHullVertices];
+    T vx[kMaxHullVertices];
+    T vy[kMaxHullVertices];
     for (int i = 0; i < count; ++i) {
-        vx[i] = static_cast<float>(hull[i] & 0xffffu);
-        vy[i] = static_cast<float>(hull[i] >> 16);
+        vx[i] = static_cast<T>(hull[i] & 0xffffu);
+        vy[i] = static_cast<T>(hull[i] >> 16);
     }
     while (count > 4) {
         int best = -1;
-        float best_area = FLT_MAX;
+        T best_area = FLT_MAX;
         for (int i = 0; i < count; ++i) {
             const int prev = (i + count - 1) % count;
             const int next = (i + 1) % count;
-            const float ax = vx[i] - vx[prev];
-            const float ay = vy[i] - vy[prev];
-            const float bx = vx[next] - vx[i];
-            const float by = vy[next] - vy[i];
-            const float area = std::fabs(ax * by - ay * bx) * 0.5f;
+            const T ax = vx[i] - vx[prev];
+            const T ay = vy[i] - vy[prev];
+            const T bx = vx[next] - vx[i];
+            const T by = vy[next] - vy[i];
+            const T area = std::fabs(ax * by - ay * bx) * 0.5f;
             if (area < best_area) {
                 best_area = area;
                 best = i;
@@ -564,7 +582,7 @@ bool hull_to_quad(const uint32_t* hull, int count, float quad[4][2]) {
         }
         --count;
     }
-    float area2 = 0.0f;
+    T area2 = 0.0f;
     for (int i = 0; i < 4; ++i) {
         const int j = (i + 1) & 3;
         area2 += vx[i] * vy[j] - vx[j] * vy[i];
@@ -572,41 +590,41 @@ bool hull_to_quad(const uint32_t* hull, int count, float quad[4][2]) {
     if (std::fabs(area2) < 24.0f) return false;
     if (area2 < 0.0f) {
         for (int i = 0; i < 2; ++i) {
-            const float tx = vx[i + 1], ty = vy[i + 1];
+            const T tx = vx[i + 1], ty = vy[i + 1];
             vx[i + 1] = vx[3 - i];
             vy[i + 1] = vy[3 - i];
             vx[3 - i] = tx;
             vy[3 - i] = ty;
         }
     }
-    float min_side = FLT_MAX, max_side = 0.0f;
+    T min_side = FLT_MAX, max_side = 0.0f;
     for (int i = 0; i < 4; ++i) {
         const int j = (i + 1) & 3;
-        const float ex = vx[j] - vx[i];
-        const float ey = vy[j] - vy[i];
-        const float len = std::sqrt(ex * ex + ey * ey);
+        const T ex = vx[j] - vx[i];
+        const T ey = vy[j] - vy[i];
+        const T len = std::sqrt(ex * ex + ey * ey);
         if (len < 4.0f) return false;
         min_side = std::fmin(min_side, len);
         max_side = std::fmax(max_side, len);
         const int pi = (i + 3) & 3;
-        const float ax = vx[i] - vx[pi];
-        const float ay = vy[i] - vy[pi];
-        const float bx = vx[j] - vx[i];
-        const float by = vy[j] - vy[i];
+        const T ax = vx[i] - vx[pi];
+        const T ay = vy[i] - vy[pi];
+        const T bx = vx[j] - vx[i];
+        const T by = vy[j] - vy[i];
         if (ax * by - ay * bx <= 0.0f) return false;
-        const float dot = ax * bx + ay * by;
-        const float n1 = std::sqrt(ax * ax + ay * ay);
-        const float n2 = std::sqrt(bx * bx + by * by);
+        const T dot = ax * bx + ay * by;
+        const T n1 = std::sqrt(ax * ax + ay * ay);
+        const T n2 = std::sqrt(bx * bx + by * by);
         if (n1 < 1e-3f || n2 < 1e-3f) return false;
         if (std::fabs(dot / (n1 * n2)) > 0.97f) return false;
     }
     if (max_side > 12.0f * min_side) return false;
-    const float cx = 0.25f * (vx[0] + vx[1] + vx[2] + vx[3]);
-    const float cy = 0.25f * (vy[0] + vy[1] + vy[2] + vy[3]);
+    const T cx = 0.25f * (vx[0] + vx[1] + vx[2] + vx[3]);
+    const T cy = 0.25f * (vy[0] + vy[1] + vy[2] + vy[3]);
     for (int i = 0; i < 4; ++i) {
-        const float dx = vx[i] - cx;
-        const float dy = vy[i] - cy;
-        const float len = std::sqrt(dx * dx + dy * dy);
+        const T dx = vx[i] - cx;
+        const T dy = vy[i] - cy;
+        const T len = std::sqrt(dx * dx + dy * dy);
         if (len > 1e-3f) {
             vx[i] += dx / len * 0.65f;
             vy[i] += dy / len * 0.65f;
@@ -620,40 +638,42 @@ bool hull_to_quad(const uint32_t* hull, int count, float quad[4][2]) {
 }
 
 // sample_bilinear :833-849
-float sample_bilinear(const uint8_t* image, int width, int height, int stride, float x, float y) {
-    if (!(x >= 0.0f && y >= 0.0f && x < static_cast<float>(width - 1) &&
-          y < static_cast<float>(height - 1))) {
+template <typename T>
+T sample_bilinear(const uint8_t* image, int width, int height, int stride, T x, T y) {
+    if (!(x >= 0.0f && y >= 0.0f && x < static_cast<T>(width - 1) &&
+          y < static_cast<T>(height - 1))) {
         return -1.0f;
     }
     const int ix = static_cast<int>(x);
     const int iy = static_cast<int>(y);
-    const float fx = x - static_cast<float>(ix);
-    const float fy = y - static_cast<float>(iy);
+    const T fx = x - static_cast<T>(ix);
+    const T fy = y - static_cast<T>(iy);
     const uint8_t* q = image + static_cast<size_t>(iy) * stride + ix;
-    const float a = q[0];
-    const float b = q[1];
-    const float c = q[stride];
-    const float d = q[stride + 1];
+    const T a = q[0];
+    const T b = q[1];
+    const T c = q[stride];
+    const T d = q[stride + 1];
     return (a * (1.0f - fx) + b * fx) * (1.0f - fy) + (c * (1.0f - fx) + d * fx) * fy;
 }
 
 // intersect_lines :851-859
-bool intersect_lines(const float li[4], const float lj[4], float* x, float* y) {
-    const float det = li[2] * lj[3] - li[3] * lj[2];
+template <typename T>
+bool intersect_lines(const T li[4], const T lj[4], T* x, T* y) {
+    const T det = li[2] * lj[3] - li[3] * lj[2];
     if (std::fabs(det) < 0.2f) return false;
-    const float di = li[2] * li[0] + li[3] * li[1];
-    const float dj = lj[2] * lj[0] + lj[3] * lj[1];
+    const T di = li[2] * li[0] + li[3] * li[1];
+    const T dj = lj[2] * lj[0] + lj[3] * lj[1];
     *x = (di * lj[3] - li[3] * dj) / det;
     *y = (li[2] * dj - di * lj[2]) / det;
     return true;
 }
 
 // directional_rise :865-874
-float directional_rise(const uint8_t* image, int width, int height, int stride, float x, float y,
-                       float dx, float dy) {
-    const float ahead = sample_bilinear(image, width, height, stride, x + dx * 0.7f, y + dy * 0.7f);
-    const float behind =
-        sample_bilinear(image, width, height, stride, x - dx * 0.7f, y - dy * 0.7f);
+template <typename T>
+T directional_rise(const uint8_t* image, int width, int height, int stride, T x, T y, T dx,
+                   T dy) {
+    const T ahead = sample_bilinear(image, width, height, stride, x + dx * 0.7f, y + dy * 0.7f);
+    const T behind = sample_bilinear(image, width, height, stride, x - dx * 0.7f, y - dy * 0.7f);
     if (ahead < 0.0f || behind < 0.0f) return 0.0f;
     return ahead - behind;
 }
@@ -671,39 +691,40 @@ T warp_tree_sum(const T* v) {
 }
 
 // fit_edge_line_warp :881-1016, one lane per position along the edge.
-bool fit_edge_line(const float quad[4][2], int edge, const uint8_t* image, const Params& p,
-                   int dim, bool first_pass, float line[4]) {
+template <typename T>
+bool fit_edge_line(const T quad[4][2], int edge, const uint8_t* image, const Params& p, int dim,
+                   bool first_pass, T line[4]) {
     const int width = p.width, height = p.height, stride = p.stride;
     const int b = (edge + 1) & 3;
-    const float ax = quad[edge][0], ay = quad[edge][1];
-    const float bx = quad[b][0], by = quad[b][1];
-    const float ex = bx - ax;
-    const float ey = by - ay;
-    const float len = std::sqrt(ex * ex + ey * ey);
+    const T ax = quad[edge][0], ay = quad[edge][1];
+    const T bx = quad[b][0], by = quad[b][1];
+    const T ex = bx - ax;
+    const T ey = by - ay;
+    const T len = std::sqrt(ex * ex + ey * ey);
     if (len < 8.0f) return false;
-    const float nx = ey / len;
-    const float ny = -ex / len;
-    const float cell = len / static_cast<float>(dim);
-    const float range = first_pass ? std::fmin(std::fmax(1.15f * cell, 1.5f), 2.5f * cell)
+    const T nx = ey / len;
+    const T ny = -ex / len;
+    const T cell = len / static_cast<T>(dim);
+    const T range = first_pass ? std::fmin(std::fmax(1.15f * cell, 1.5f), 2.5f * cell)
                                    : std::fmin(std::fmax(0.30f * cell, 0.8f), 2.0f);
     const int half =
         std::min(std::max(2, static_cast<int>(std::ceil(range / 0.75f))), kFitProbeHalf);
     const int probes = 2 * half + 1;
-    const float step = range / static_cast<float>(half);
+    const T step = range / static_cast<T>(half);
     const int samples = std::min(std::max(static_cast<int>(len / 6.0f), 8), 16);
 
-    float vmx[32] = {}, vmy[32] = {}, vmxx[32] = {}, vmxy[32] = {}, vmyy[32] = {};
+    T vmx[32] = {}, vmy[32] = {}, vmxx[32] = {}, vmxy[32] = {}, vmyy[32] = {};
     int vused[32] = {};
     for (int lane = 0; lane < samples; ++lane) {
-        const float alpha = static_cast<float>(lane + 1) / static_cast<float>(samples + 1);
-        const float px = ax + alpha * ex;
-        const float py = ay + alpha * ey;
-        float mags[kFitProbeHalf * 2 + 1];
-        float best_mag = 0.0f;
+        const T alpha = static_cast<T>(lane + 1) / static_cast<T>(samples + 1);
+        const T px = ax + alpha * ex;
+        const T py = ay + alpha * ey;
+        T mags[kFitProbeHalf * 2 + 1];
+        T best_mag = 0.0f;
         int best = -1;
         for (int i = 0; i < probes; ++i) {
-            const float t = step * static_cast<float>(i - half);
-            const float mag =
+            const T t = step * static_cast<T>(i - half);
+            const T mag =
                 directional_rise(image, width, height, stride, px + nx * t, py + ny * t, nx, ny);
             mags[i] = mag;
             if (mag > best_mag) {
@@ -712,10 +733,10 @@ bool fit_edge_line(const float quad[4][2], int edge, const uint8_t* image, const
             }
         }
         if (first_pass && best > 2) {
-            const float accept = 0.70f * best_mag;
+            const T accept = 0.70f * best_mag;
             for (int i = 1; i + 1 < best; ++i) {
                 if (mags[i] < accept || mags[i] < mags[i - 1] || mags[i] < mags[i + 1]) continue;
-                float valley = FLT_MAX;
+                T valley = FLT_MAX;
                 for (int k = i + 1; k < best; ++k) valley = std::fmin(valley, mags[k]);
                 if (valley < 0.5f * mags[i]) {
                     best = i;
@@ -725,19 +746,19 @@ bool fit_edge_line(const float quad[4][2], int edge, const uint8_t* image, const
             }
         }
         if (best >= 0 && best_mag >= 6.0f) {
-            float t = step * static_cast<float>(best - half);
+            T t = step * static_cast<T>(best - half);
             if (best > 0 && best < probes - 1) {
-                const float m0 = directional_rise(image, width, height, stride,
-                                                  px + nx * (t - step), py + ny * (t - step), nx, ny);
-                const float m2 = directional_rise(image, width, height, stride,
-                                                  px + nx * (t + step), py + ny * (t + step), nx, ny);
-                const float den = m0 - 2.0f * best_mag + m2;
+                const T m0 = directional_rise(image, width, height, stride, px + nx * (t - step),
+                                              py + ny * (t - step), nx, ny);
+                const T m2 = directional_rise(image, width, height, stride, px + nx * (t + step),
+                                              py + ny * (t + step), nx, ny);
+                const T den = m0 - 2.0f * best_mag + m2;
                 if (den < -1e-3f) {
                     t += std::fmin(std::fmax(0.5f * (m0 - m2) / den, -0.5f), 0.5f) * step;
                 }
             }
-            const float x = px + nx * t;
-            const float y = py + ny * t;
+            const T x = px + nx * t;
+            const T y = py + ny * t;
             vmx[lane] = x;
             vmy[lane] = y;
             vmxx[lane] = x * x;
@@ -746,19 +767,19 @@ bool fit_edge_line(const float quad[4][2], int edge, const uint8_t* image, const
             vused[lane] = 1;
         }
     }
-    const float mx = warp_tree_sum(vmx), my = warp_tree_sum(vmy);
-    const float mxx = warp_tree_sum(vmxx), mxy = warp_tree_sum(vmxy), myy = warp_tree_sum(vmyy);
+    const T mx = warp_tree_sum(vmx), my = warp_tree_sum(vmy);
+    const T mxx = warp_tree_sum(vmxx), mxy = warp_tree_sum(vmxy), myy = warp_tree_sum(vmyy);
     const int used = warp_tree_sum(vused);
     if (used < 4) return false;
-    const float inv = 1.0f / static_cast<float>(used);
-    const float cx = mx * inv;
-    const float cy = my * inv;
-    const float cxx = mxx * inv - cx * cx;
-    const float cxy = mxy * inv - cx * cy;
-    const float cyy = myy * inv - cy * cy;
-    const float theta = 0.5f * bdmath::atan2(2.0f * cxy, cxx - cyy);
-    float s, c;
-    bdmath::sincos(theta, &s, &c);
+    const T inv = 1.0f / static_cast<T>(used);
+    const T cx = mx * inv;
+    const T cy = my * inv;
+    const T cxx = mxx * inv - cx * cx;
+    const T cxy = mxy * inv - cx * cy;
+    const T cyy = myy * inv - cy * cy;
+    const T theta = 0.5f * fm_atan2(2.0f * cxy, cxx - cyy);
+    T s, c;
+    fm_sincos(theta, &s, &c);
     line[0] = cx;
     line[1] = cy;
     line[2] = -s;
@@ -767,30 +788,31 @@ bool fit_edge_line(const float quad[4][2], int edge, const uint8_t* image, const
 }
 
 // apply_refined_lines :1021-1076
-float apply_refined_lines(float quad[4][2], const float lines[4][4], const int have[4]) {
+template <typename T>
+T apply_refined_lines(T quad[4][2], const T lines[4][4], const int have[4]) {
     int line_count = 0;
     for (int i = 0; i < 4; ++i) line_count += have[i] ? 1 : 0;
     if (line_count < 3) return 0.0f;
-    float refined[4][2];
+    T refined[4][2];
     for (int i = 0; i < 4; ++i) {
         refined[i][0] = quad[i][0];
         refined[i][1] = quad[i][1];
     }
-    float extent = 0.0f;
+    T extent = 0.0f;
     for (int i = 0; i < 4; ++i) {
         const int j = (i + 1) & 3;
-        extent = std::fmax(extent, bdmath::hypot(quad[j][0] - quad[i][0], quad[j][1] - quad[i][1]));
+        extent = std::fmax(extent, fm_hypot(quad[j][0] - quad[i][0], quad[j][1] - quad[i][1]));
     }
-    const float max_shift = std::fmin(std::fmax(0.15f * extent, 4.0f), 16.0f);
-    float moved = 0.0f;
+    const T max_shift = std::fmin(std::fmax(0.15f * extent, 4.0f), 16.0f);
+    T moved = 0.0f;
     for (int i = 0; i < 4; ++i) {
         const int j = (i + 1) & 3;
         if (!have[i] || !have[j]) continue;
-        float x, y;
+        T x, y;
         if (!intersect_lines(lines[i], lines[j], &x, &y)) continue;
         const int corner = j;
-        const float dx = x - quad[corner][0];
-        const float dy = y - quad[corner][1];
+        const T dx = x - quad[corner][0];
+        const T dy = y - quad[corner][1];
         if (dx * dx + dy * dy > max_shift * max_shift) continue;
         refined[corner][0] = x;
         refined[corner][1] = y;
@@ -798,11 +820,11 @@ float apply_refined_lines(float quad[4][2], const float lines[4][4], const int h
     }
     for (int i = 0; i < 4; ++i) {
         const int j = (i + 1) & 3;
-        if (bdmath::hypot(refined[j][0] - refined[i][0], refined[j][1] - refined[i][1]) < 3.0f) {
+        if (fm_hypot(refined[j][0] - refined[i][0], refined[j][1] - refined[i][1]) < 3.0f) {
             return 0.0f;
         }
     }
-    float area2 = 0.0f;
+    T area2 = 0.0f;
     for (int i = 0; i < 4; ++i) {
         const int j = (i + 1) & 3;
         area2 += refined[i][0] * refined[j][1] - refined[j][0] * refined[i][1];
@@ -816,17 +838,19 @@ float apply_refined_lines(float quad[4][2], const float lines[4][4], const int h
 }
 
 // The 32 probe directions of k_fit_quads :1139-1142.
-void probe_directions(float ux[kFitDirections], float uy[kFitDirections]) {
+template <typename T>
+void probe_directions(T ux[kFitDirections], T uy[kFitDirections]) {
     for (int dir = 0; dir < kFitDirections; ++dir) {
-        const float angle =
-            6.28318530718f * static_cast<float>(dir) / static_cast<float>(kFitDirections);
-        bdmath::sincos(angle, &uy[dir], &ux[dir]);
+        const T angle =
+            two_pi(T()) * static_cast<T>(dir) / static_cast<T>(kFitDirections);
+        fm_sincos(angle, &uy[dir], &ux[dir]);
     }
 }
 
 // k_fit_quads :1081-1241 for one candidate.  Returns true when the hull gave
 // a quad (counts[3]); fills hull_out and out (8 floats each).
-bool fit_quad(const bdo_frame& f, const uint8_t* gray, uint32_t root, float* hull_out, float* out) {
+template <typename T>
+bool fit_quad(const bdo_frame& f, const uint8_t* gray, uint32_t root, T* hull_out, T* out) {
     const Params& p = f.p;
     const int x0 = static_cast<int>(f.bbox[root * 4 + 0]);
     const int y0 = static_cast<int>(f.bbox[root * 4 + 1]);
@@ -838,17 +862,17 @@ bool fit_quad(const bdo_frame& f, const uint8_t* gray, uint32_t root, float* hul
     std::vector<uint32_t> boundary(2 * kMaxBoundaryRows, kNone);
     row_extremes(f, root, x0, x1, y0, rows, kept, boundary.data());
 
-    float ux[kFitDirections], uy[kFitDirections];
+    T ux[kFitDirections], uy[kFitDirections];
     probe_directions(ux, uy);
     uint32_t extreme[kFitDirections];
     for (int dir = 0; dir < kFitDirections; ++dir) {
-        float best_dot = -FLT_MAX;
+        T best_dot = -FLT_MAX;
         uint32_t best_point = kNone;
         for (int i = 0; i < points; ++i) {
             const uint32_t q = boundary[i];
             if (q == kNone) continue;
-            const float d = static_cast<float>(q & 0xffffu) * ux[dir] +
-                            static_cast<float>(q >> 16) * uy[dir];
+            const T d =
+                static_cast<T>(q & 0xffffu) * ux[dir] + static_cast<T>(q >> 16) * uy[dir];
             if (d > best_dot) {
                 best_dot = d;
                 best_point = q;
@@ -866,7 +890,7 @@ bool fit_quad(const bdo_frame& f, const uint8_t* gray, uint32_t root, float* hul
     }
     while (hc > 1 && hull[0] == hull[hc - 1]) --hc;
 
-    float quad[4][2];
+    T quad[4][2];
     if (!hull_to_quad(hull, hc, quad)) return false;
     for (int i = 0; i < 4; ++i) {
         hull_out[i * 2 + 0] = quad[i][0];
@@ -874,12 +898,12 @@ bool fit_quad(const bdo_frame& f, const uint8_t* gray, uint32_t root, float* hul
     }
     if (p.refine_edges) {
         for (int iteration = 0; iteration < kFitIterations; ++iteration) {
-            float lines[4][4] = {};
+            T lines[4][4] = {};
             int have[4];
             for (int e = 0; e < 4; ++e) {
                 have[e] = fit_edge_line(quad, e, gray, p, p.dim, iteration == 0, lines[e]) ? 1 : 0;
             }
-            const float moved = apply_refined_lines(quad, lines, have);
+            const T moved = apply_refined_lines(quad, lines, have);
             if (moved < 0.15f) break;
         }
     }
@@ -1055,7 +1079,8 @@ bool decode_candidate(const uint8_t* gray, const Params& p, const float* q, cons
 
 // --- 9. finalize :1542-1601 and the host homography :1739-1774 -------------
 
-void fill_homography(const float corners[8], float H[9]) {
+template <typename In, typename Out>
+void fill_homography(const In corners[8], Out H[9]) {
     const double x0 = corners[0], y0 = corners[1];
     const double x1 = corners[2], y1 = corners[3];
     const double x2 = corners[4], y2 = corners[5];
@@ -1076,15 +1101,15 @@ void fill_homography(const float corners[8], float H[9]) {
     const double e = y3 - y0 + h * y3;
     const double w = g + h + 2.0;
     const double inv = (std::fabs(w) > 1e-12) ? 1.0 / w : 0.0;
-    H[0] = static_cast<float>(a * inv);
-    H[1] = static_cast<float>(b * inv);
-    H[2] = static_cast<float>((a + b + 2.0 * x0) * inv);
-    H[3] = static_cast<float>(d * inv);
-    H[4] = static_cast<float>(e * inv);
-    H[5] = static_cast<float>((d + e + 2.0 * y0) * inv);
-    H[6] = static_cast<float>(g * inv);
-    H[7] = static_cast<float>(h * inv);
-    H[8] = static_cast<float>(w * inv);
+    H[0] = static_cast<Out>(a * inv);
+    H[1] = static_cast<Out>(b * inv);
+    H[2] = static_cast<Out>((a + b + 2.0 * x0) * inv);
+    H[3] = static_cast<Out>(d * inv);
+    H[4] = static_cast<Out>(e * inv);
+    H[5] = static_cast<Out>((d + e + 2.0 * y0) * inv);
+    H[6] = static_cast<Out>(g * inv);
+    H[7] = static_cast<Out>(h * inv);
+    H[8] = static_cast<Out>(w * inv);
 }
 
 void finalize(bdo_frame& f) {
@@ -1296,6 +1321,20 @@ int32_t bdo_detect_many(int32_t frames, const uint8_t* const* grays, const int32
     for (auto& t : pool) t.join();
     return 0;
 }
+
+int32_t bdo_refit64(const bdo_frame* f, const uint8_t* gray, double* hull_out, double* quads_out) {
+    const int n = static_cast<int>(f->candidates.size());
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    for (int ci = 0; ci < n; ++ci) {
+        double* hq = hull_out + static_cast<size_t>(ci) * 8;
+        double* q = quads_out + static_cast<size_t>(ci) * 8;
+        for (int k = 0; k < 8; ++k) hq[k] = q[k] = nan;
+        fit_quad(*f, gray, f->candidates[ci], hq, q);
+    }
+    return n;
+}
+
+void bdo_homography64(const double corners[8], double H[9]) { fill_homography(corners, H); }
 
 float bdo_sinf(float x) { return bdmath::sin(x); }
 float bdo_cosf(float x) { return bdmath::cos(x); }

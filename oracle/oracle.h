@@ -75,6 +75,18 @@ int32_t bdo_detect_many(int32_t frames, const uint8_t* const* grays, const int32
                         int32_t threads, bd_detection* out, int32_t max_detections,
                         int32_t* counts);
 
+// FP64 re-fit: the hull, quad and edge-refinement steps of every candidate
+// evaluated in double precision (C library sin/cos/atan2/hypot), from the
+// frame's integer stages.  `gray` must be the image the frame was run on.
+// hull_out and quads_out hold candidate_count * 8 doubles (NaN when the
+// candidate gives no quad).  Returns candidate_count.
+int32_t bdo_refit64(const bdo_frame* frame, const uint8_t* gray, double* hull_out,
+                    double* quads_out);
+
+// The host homography of the result records (reference fill_homography,
+// gpu_detector.cu:1739-1774) from FP64 corners, kept in FP64.
+void bdo_homography64(const double corners[8], double H[9]);
+
 // The deterministic math helpers, exported for the accuracy test.
 float bdo_sinf(float x);
 float bdo_cosf(float x);

@@ -83,6 +83,9 @@ def lib() -> ctypes.CDLL:
             [ctypes.POINTER(Config), ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
              ctypes.c_void_p]
         L.bdo_detect_many.restype = ctypes.c_int32
+        L.bdo_refit64.argtypes = [ctypes.c_void_p] * 4
+        L.bdo_refit64.restype = ctypes.c_int32
+        L.bdo_homography64.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         for name in ("bdo_sinf", "bdo_cosf"):
             getattr(L, name).argtypes = [ctypes.c_float]
             getattr(L, name).restype = ctypes.c_float
@@ -140,6 +143,18 @@ class Frame:
         lib().bdo_counts(self._h, c.ctypes.data)
         return c
 
+    def refit64(self, gray: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """FP64 re-fit of every candidate: (hull quads, refined quads), each
+        float64[candidate_count, 8] with NaN rows where no quad was fitted.
+        `gray` must be the image this frame was run on."""
+        n = self.candidate_count
+        hq = np.full((max(n, 1), 8), np.nan)
+        q = np.full((max(n, 1), 8), np.nan)
+        img = np.ascontiguousarray(gray, dtype=np.uint8)
+        assert img.shape == (self.height, self.width)
+        lib().bdo_refit64(self._h, img.ctypes.data, hq.ctypes.data, q.ctypes.data)
+        return hq[:n], q[:n]
+
     def stage(self, name: str) -> np.ndarray:
         size = lib().bdo_stage(self._h, name.encode(), None, 0)
         if size < 0:
@@ -148,6 +163,14 @@ class Frame:
         out = np.zeros(size // dt.itemsize, dtype=dt)
         lib().bdo_stage(self._h, name.encode(), out.ctypes.data, size)
         return out
+
+
+def homography64(corners: np.ndarray) -> np.ndarray:
+    """The result-record homography from FP64 corners, in FP64 (float64[9])."""
+    c = np.ascontiguousarray(corners, dtype=np.float64).reshape(8)
+    h = np.zeros(9, dtype=np.float64)
+    lib().bdo_homography64(c.ctypes.data, h.ctypes.data)
+    return h
 
 
 def detect(gray: np.ndarray, family: int = 0, config: Config | None = None) -> np.ndarray:

@@ -62,3 +62,31 @@ def kat_multiple_frame():
         poses[tid] = pose
         img = np.minimum(img, scenes.render_tag(0, tid, 1280, 720, pose))
     return img, poses
+
+
+def refit64_errors(frame, gray, quads32, hulls32, decodes):
+    """Per decoded candidate: (max corner distance in px between the FP32
+    quad and the oracle's FP64 re-fit, whether the FP64 hull quad is the same
+    within 1e-3 px, relative max-abs difference of the result homography
+    built from the FP32 corners and from the FP64 corners, in FP64)."""
+    import oracle
+    n = frame.candidate_count
+    h64, q64 = frame.refit64(gray)
+    q32 = np.asarray(quads32, dtype=np.float64)[:n * 8].reshape(n, 8)
+    h32 = np.asarray(hulls32, dtype=np.float64)[:n * 8].reshape(n, 8)
+    out = []
+    for ci in range(n):
+        if decodes["id"][ci] < 0 or np.isnan(q64[ci, 0]) or np.isnan(q32[ci, 0]):
+            continue
+        err = float(np.hypot(q32[ci, 0::2] - q64[ci, 0::2], q32[ci, 1::2] - q64[ci, 1::2]).max())
+        same_hull = bool(np.abs(h32[ci] - h64[ci]).max() < 1e-3)
+        rel = float("nan")
+        c32 = decodes["corners"][ci].astype(np.float64)
+        for r in range(4):  # the decoded rotation of the refined quad
+            if np.array_equal(np.roll(q32[ci].reshape(4, 2), -r, axis=0).reshape(8), c32):
+                hh64 = oracle.homography64(np.roll(q64[ci].reshape(4, 2), -r, axis=0).reshape(8))
+                hh32 = oracle.homography64(c32)
+                rel = float(np.abs(hh32 - hh64).max() / np.abs(hh64).max())
+                break
+        out.append((err, same_hull, rel))
+    return out

@@ -337,3 +337,30 @@ def test_pipeline_runner_checks_and_results():
         n, want = oracle.Frame(img, fam).detections()
         assert found[0, fam] == n
         same_records(out[0, fam, :n], want)
+
+
+def test_gpu_corners_against_fp64_refit():
+    """The GPU's FP32 quads against the oracle's FP64 re-fit of the same
+    candidates (hull, quad and edge refinement in double precision): the
+    error statement of test_refit64.py, made on the CUDA results."""
+    from helpers import refit64_errors
+    rows = []
+    for i in range(8):
+        img, _ = scenes.render_scene(scenes.MIXED_1280, i, 1280, 800)
+        for fam in (0, 1):
+            det = bdcudatag.Detector(fam, 1280, 800)
+            det.detect(img)
+            ref = oracle.Frame(img, fam)
+            nc = ref.candidate_count
+            q = det.stage("quads")[fam * ref.max_candidates * 8:][:nc * 8]
+            hq = det.stage("hull_quads")[:nc * 8]
+            dg = det.stage("decodes")[fam * ref.max_candidates:][:nc]
+            rows += refit64_errors(ref, img, q, hq, dg)
+    assert len(rows) >= 50
+    err = np.array([r[0] for r in rows])
+    same = np.array([r[1] for r in rows])
+    rel = np.array([r[2] for r in rows])
+    assert same.mean() >= 0.85
+    assert np.median(err[same]) < 5e-3 and err[same].max() < 0.1
+    assert np.mean(err > 0.1) <= 0.05
+    assert np.nanmedian(rel[same]) < 1e-4
