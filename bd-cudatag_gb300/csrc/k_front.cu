@@ -222,9 +222,10 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
 //    band-local connected components, for one band of 8 rows; warp w owns
 //    row y0 + w.
 //
-//    The runs of a band are unioned in shared memory (same-row fragments and
-//    8-connected runs of consecutive rows inside the band), and area / bbox
-//    are aggregated per band-local root with shared-memory atomics.  Global
+//    The runs of a band are labelled in shared memory (same-row fragments and
+//    8-connected runs of consecutive rows inside the band, by hooking and
+//    flattening rounds), and area / bbox are aggregated per band-local root
+//    with shared-memory atomics.  Global
 //    memory then receives one parent link per run (to its band-local root)
 //    and one aggregate per band-local root; k_merge only unions across band
 //    boundaries and k_region_stats folds band roots into global roots.  The
@@ -236,31 +237,6 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
 //    first row to the row above; only a single row longer than `cap` sends
 //    the band back to one root per run and full merging in k_merge.
 // ===========================================================================
-
-__device__ __forceinline__ uint32_t s_find(uint32_t* par, uint32_t x) {
-    for (;;) {
-        const uint32_t p = par[x];
-        if (p == x) return x;
-        const uint32_t gp = par[p];
-        par[x] = gp;
-        x = gp;
-    }
-}
-
-__device__ __forceinline__ void s_union(uint32_t* par, uint32_t a, uint32_t b) {
-    a = s_find(par, a);
-    b = s_find(par, b);
-    while (a != b) {
-        if (a > b) {
-            const uint32_t t = a;
-            a = b;
-            b = t;
-        }
-        const uint32_t old = atomicMin(&par[b], a);
-        if (old == a) break;
-        b = s_find(par, old);
-    }
-}
 
 __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restrict__ b,
                                                        const FrameIO* __restrict__ io, int cap,
@@ -501,7 +477,6 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
                 sm_par[i] = i;
                 sm_row[i] = static_cast<uint8_t>(row);
             }
-            sm_area[i] = 0u;
             sm_minx[i] = 0xffffffffu;
             sm_maxx[i] = 0u;
             sm_rows[i] = 0u;
@@ -509,23 +484,44 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
         __syncthreads();
 
         // Unions inside the segment (the reference's k_merge_runs rules).
-        if (w >= r0 && w < r1 && w < rows) {
+        // First the same-row rule: consecutive fragments that touch (a run
+        // cut at word boundaries, or runs one pixel apart) form one group,
+        // and every fragment points straight at the group's first fragment.
+        // Linking each fragment to its left neighbour instead builds chains
+        // as long as the row, which every later find walks.  Row 0 of the
+        // frame is never merged, not even its word-split fragments
+        // (reference k_merge_runs :514 returns for y <= 0).
+        if (w >= r0 && w < r1 && w < rows && y0 + w > 0) {
             const uint32_t n = s_rowtot[w];
             const uint32_t base = s_rowoff[w] - seg_off;
-            const uint32_t prev_n = w > r0 ? s_rowtot[w - 1] : 0u;
-            const uint32_t pbase = w > r0 ? s_rowoff[w - 1] - seg_off : 0u;
-            for (uint32_t i = lane; i < n; i += 32) {
-                const uint32_t run = sm_run[base + i];
+            uint32_t carry = 0;  // group head of the previous chunk's last fragment
+            for (uint32_t c = 0; c < n; c += 32) {
+                const uint32_t i = c + static_cast<uint32_t>(lane);
+                bool head = true;
+                if (i < n && i > 0) {
+                    const int x0 = static_cast<int>(sm_run[base + i] & 0xffffu);
+                    const int px1 = static_cast<int>(sm_run[base + i - 1] >> 16);
+                    head = px1 + 1 < x0;
+                }
+                const uint32_t upto = __ballot_sync(kFull, head) & (kFull >> (31 - lane));
+                const uint32_t h = upto ? c + 31u - static_cast<uint32_t>(__clz(upto)) : carry;
+                if (i < n) sm_par[base + i] = base + h;
+                carry = __shfl_sync(kFull, h, 31);
+            }
+        }
+        // Then the rows meet: run i of row r > r0 overlaps (8-connected) the
+        // runs [first, first + count) of row r - 1, kept in sm_area[i] until
+        // the roots pass needs it.
+        for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
+            const int row = sm_row[i];
+            uint32_t list = 0;
+            if (row > r0) {
+                const uint32_t run = sm_run[i];
                 const int x0 = static_cast<int>(run & 0xffffu);
                 const int x1 = static_cast<int>(run >> 16);
-                // Row 0 of the frame is never merged, not even its word-split
-                // fragments (reference k_merge_runs :514 returns for y <= 0).
-                if (i > 0 && y0 + w > 0) {
-                    const int px1 = static_cast<int>(sm_run[base + i - 1] >> 16);
-                    if (px1 + 1 >= x0) s_union(sm_par, base + i, base + i - 1);
-                }
-                if (prev_n == 0) continue;
-                int lo2 = 0, hi2 = static_cast<int>(prev_n) - 1, first = static_cast<int>(prev_n);
+                const uint32_t pbase = s_rowoff[row - 1] - seg_off;
+                const int prev_n = static_cast<int>(s_rowtot[row - 1]);
+                int lo2 = 0, hi2 = prev_n - 1, first = prev_n;
                 while (lo2 <= hi2) {
                     const int mid = (lo2 + hi2) >> 1;
                     if (static_cast<int>(sm_run[pbase + mid] >> 16) >= x0 - 1) {
@@ -535,30 +531,53 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
                         lo2 = mid + 1;
                     }
                 }
-                for (int k = first; k < static_cast<int>(prev_n); ++k) {
-                    const int px0 = static_cast<int>(sm_run[pbase + k] & 0xffffu);
-                    if (px0 > x1 + 1) break;
-                    s_union(sm_par, base + i, pbase + k);
-                }
+                int k = first;
+                while (k < prev_n && static_cast<int>(sm_run[pbase + k] & 0xffffu) <= x1 + 1) ++k;
+                list = (pbase + static_cast<uint32_t>(first)) | (static_cast<uint32_t>(k - first) << 16);
             }
+            sm_area[i] = list;
         }
         __syncthreads();
 
-        // Flatten the forest by pointer jumping (parents have smaller
-        // indices, so every value written is an ancestor): log-depth rounds
-        // instead of each run walking its whole chain.
+        // Components by hooking and flattening rounds.  A round hooks, for
+        // every overlapping pair with different parents, the larger parent
+        // under the smaller one (atomicMin), then flattens the forest by
+        // pointer jumping, so every round starts from roots.  Parents only
+        // decrease and always stay in the component, so the rounds end; the
+        // last one finds every pair under one root, which is the component's
+        // smallest index, as with the reference's union-find.  Each round
+        // merges every tree with a neighbour: 3-5 rounds on 8-row bands of
+        // camera frames, where concurrent union-find walked chains of
+        // hundreds of links.
         for (;;) {
-            int changed = 0;
+            int hooked = 0;
             for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
-                const uint32_t p = sm_par[i];
-                const uint32_t gp = sm_par[p];
-                if (gp != p) {
-                    sm_par[i] = gp;
-                    changed = 1;
+                const uint32_t list = sm_area[i];
+                const uint32_t a = sm_par[i];
+                for (uint32_t k = list & 0xffffu, k_end = k + (list >> 16); k < k_end; ++k) {
+                    const uint32_t p = sm_par[k];
+                    if (p != a) {
+                        atomicMin(&sm_par[max(a, p)], min(a, p));
+                        hooked = 1;
+                    }
                 }
             }
-            if (!__syncthreads_or(changed)) break;
+            if (!__syncthreads_or(hooked)) break;
+            for (;;) {
+                int changed = 0;
+                for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
+                    const uint32_t p = sm_par[i];
+                    const uint32_t gp = sm_par[p];
+                    if (gp != p) {
+                        sm_par[i] = gp;
+                        changed = 1;
+                    }
+                }
+                if (!__syncthreads_or(changed)) break;
+            }
         }
+        for (uint32_t i = tid; i < seg_n; i += blockDim.x) sm_area[i] = 0u;
+        __syncthreads();
 
         // Segment roots (its smallest slot) and their area / bbox.
         for (uint32_t i = tid; i < seg_n; i += blockDim.x) {

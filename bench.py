@@ -675,7 +675,9 @@ def bench_ours(args, rank, world, local_rank):
         "refine": refine,
         "mixed_size_batches": mixed,
         "clocks": clocks.summary(),
-        "gpu_launches": 9 * args.steps,
+        # k_stats, k_binarize_runs, k_merge, k_region_stats, k_cand_count,
+        # k_fit_decode (+ k_fit_decode_big when the split is on), k_finalize
+        "gpu_launches": (8 if plans[0].launch()["quad_split"] > 0 else 7) * args.steps,
     }
     print(json.dumps(line), flush=True)
 
