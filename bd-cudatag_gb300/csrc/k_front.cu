@@ -682,7 +682,9 @@ __global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b,
                                          static_cast<uint32_t>(y * row_cap),
                                          static_cast<uint32_t>((y - 1) * row_cap), false);
             }
-            __syncthreads();  // the next pair reuses the buffers
+            // The next pair reuses the buffers.  After the last pair, threads
+            // without runs leave at once instead of waiting for the unions.
+            if (starts & (starts - 1u)) __syncthreads();
         }
         return;
     }
