@@ -178,9 +178,9 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     mark(3);
     k_region_stats<<<bands, 256, 0, s>>>(dd, io);
     mark(4);
-    k_cand_count<<<bands, 256, 0, s>>>(dd, io);
-    mark(5);
     const int split = lc.quad_split;
+    k_cand_count<<<bands, 256, 0, s>>>(dd, io, split);
+    mark(5);
     int cands = 0;
     for (int f = 0; f < hd.frames; ++f) cands += hd.f[f].max_candidates;
     const int big_grid = std::max(1, std::min(cands, sm_count));

@@ -794,7 +794,7 @@ __device__ __forceinline__ uint32_t band_slot(const uint32_t* rowoff, int y0, ui
 // tag-like filter, and each candidate's rank among the band's candidates
 // of its area bin.
 __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict__ b,
-                                                    const FrameIO* __restrict__ io) {
+                                                    const FrameIO* __restrict__ io, int split_px) {
     __shared__ uint32_t s_rowoff[kTile + 1];
     __shared__ uint32_t s_wbin[8][64];
     __shared__ uint32_t s_run[64];
@@ -803,7 +803,7 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     __shared__ uint32_t s_base[64];
     __shared__ uint32_t s_cprefix[kMaxBandsPerFrame + 1];  // candidates before each band
     __shared__ uint32_t s_warp_sum[8];
-    __shared__ uint32_t s_ncand, s_limit;
+    __shared__ uint32_t s_ncand, s_limit, s_nbig;
     __shared__ int s_last;
 
     const int tid = threadIdx.x;
@@ -909,6 +909,7 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
         st->counts[0] = pos;
         s_limit = min(pos, static_cast<uint32_t>(d.max_candidates));
         st->n_candidates = s_limit;
+        s_nbig = 0;
     }
 
     // Placement (reference k_order_candidates :642-654): candidate j of the
@@ -946,8 +947,17 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
         const uint32_t meta = __ldcg(&d.cand_meta[slot]);
         const uint32_t cbin = meta >> 24;
         const uint32_t pos = s_base[cbin] + __ldcg(&d.band_bins[lo * 64 + cbin]) + (meta & 0xffffffu);
-        if (pos < limit) d.candidates[pos] = slot;
+        if (pos < limit) {
+            d.candidates[pos] = slot;
+            // The CTA path's work list: big candidates, listed once here
+            // instead of found by every CTA of k_fit_decode_big.
+            if (big_candidate(reinterpret_cast<const uint4*>(d.bbox)[slot], split_px)) {
+                d.big[atomicAdd(&s_nbig, 1u)] = pos;
+            }
+        }
     }
+    __syncthreads();
+    if (tid == 0) st->n_big = s_nbig;
 }
 
 }  // namespace bdgb

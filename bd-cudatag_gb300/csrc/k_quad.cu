@@ -854,10 +854,6 @@ __device__ __forceinline__ void row_extremes(const FrameDesc& d, uint32_t root, 
 
 // Whether a candidate goes to the CTA path: a bounding-box side above
 // split_px (0: never).  Both fit-and-decode kernels use this test.
-__device__ __forceinline__ bool big_candidate(uint4 bb, int split_px) {
-    return split_px > 0 && max(bb.z - bb.x, bb.w - bb.y) + 1 > static_cast<uint32_t>(split_px);
-}
-
 __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uint8_t* __restrict__ gray,
                                   int64_t stride, bool quad_ok, int lane, const float* cell_uv,
                                   QuadSmem& sm);
@@ -1054,7 +1050,8 @@ __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uin
 // refine the quad of family slot s (one warp per edge, in place of one lane
 // group per edge), and warps 2s / 2s+1 decode the refined / hull quad of
 // slot s (the hull result is used only when no refined rotation decodes).
-// CTA c takes the big candidates of rank c, c + grid, ... in work-list order.
+// CTA c takes big candidates c, c + grid, ... of the lists k_cand_count
+// wrote (FrameDesc::big).
 __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __restrict__ b,
                                                         const FrameIO* __restrict__ io, int split_px) {
     constexpr int kWarps = 8;
@@ -1074,9 +1071,6 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
     __shared__ VariantResult s_res[4];
     __shared__ int s_best[4];
     __shared__ int s_prefix[kMaxFrames + 1];
-    __shared__ int s_wcount[kWarps];
-    __shared__ int s_work[256];
-    __shared__ int s_nwork;
     __shared__ float s_uv[2][8];
 
     const int tid = threadIdx.x;
@@ -1089,10 +1083,9 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
         int run = 0;
         for (int f = 0; f < b->frames; ++f) {
             s_prefix[f] = run;
-            run += static_cast<int>(b->f[f].state->n_candidates);
+            run += static_cast<int>(b->f[f].state->n_big);
         }
         s_prefix[b->frames] = run;
-        s_nwork = 0;
     }
     __syncthreads();
     const int total = s_prefix[b->frames];
@@ -1103,42 +1096,14 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
         bdmath::sincos(angle, &uy, &ux);
     }
 
-    int running = 0;  // big candidates before this chunk
-    for (int base = 0; base < total; base += blockDim.x) {
-        // This CTA's share of the chunk's big candidates.
-        const int cand = base + tid;
-        bool big = false;
-        if (cand < total) {
-            int fi = 0;
-            while (s_prefix[fi + 1] <= cand) ++fi;
-            const FrameDesc& d = b->f[fi];
-            const uint32_t root = d.candidates[cand - s_prefix[fi]];
-            big = big_candidate(reinterpret_cast<const uint4*>(d.bbox)[root], split_px);
-        }
-        const uint32_t wb = __ballot_sync(kFull, big);
-        if (lane == 0) s_wcount[warp] = __popc(wb);
-        __syncthreads();
-        int before = running, chunk = 0;
-        for (int w = 0; w < kWarps; ++w) {
-            if (w < warp) before += s_wcount[w];
-            chunk += s_wcount[w];
-        }
-        if (big) {
-            const int rank = before + __popc(wb & lanemask_lt());
-            if (rank % static_cast<int>(gridDim.x) == static_cast<int>(blockIdx.x)) {
-                s_work[atomicAdd(&s_nwork, 1)] = cand;
-            }
-        }
-        running += chunk;
-        __syncthreads();
-        const int nwork = s_nwork;
-
-        for (int w = 0; w < nwork; ++w) {
-            const int item = s_work[w];
+    // Big candidate k of the batch (frames in order, each frame's list as
+    // k_cand_count wrote it) goes to CTA k % grid.
+    for (int item = blockIdx.x; item < total; item += gridDim.x) {
+        {
             int fi = 0;
             while (s_prefix[fi + 1] <= item) ++fi;
             const FrameDesc& d = b->f[fi];
-            const int ci = item - s_prefix[fi];
+            const int ci = static_cast<int>(d.big[item - s_prefix[fi]]);
             const int mc = d.max_candidates;
             const uint8_t* __restrict__ gray = io[fi].gray;
             const int64_t stride = io[fi].stride;
@@ -1300,12 +1265,8 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
             }
             __syncthreads();
         }
-        __syncthreads();
-        if (tid == 0) s_nwork = 0;
-        __syncthreads();
     }
 }
-
 
 size_t quad_smem_per_warp() { return sizeof(QuadSmem); }
 

@@ -30,6 +30,12 @@ __device__ __forceinline__ int frame_of_band(const BatchDesc* __restrict__ b, in
     return lo;
 }
 
+// A candidate whose bounding box has a side above `split_px` pixels is fitted
+// and decoded by a whole CTA (k_fit_decode_big); 0 turns the split off.
+__device__ __forceinline__ bool big_candidate(uint4 bb, int split_px) {
+    return split_px > 0 && max(bb.z - bb.x, bb.w - bb.y) + 1 > static_cast<uint32_t>(split_px);
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     return (1u << (threadIdx.x & 31)) - 1u;
 }

@@ -41,6 +41,7 @@ struct FrameState {
     uint32_t done_stats;     // CTAs of the stats stage finished
     uint32_t done_cands;     // CTAs of the candidate-count stage finished
     uint32_t n_candidates;   // min(counts[0], max_candidates)
+    uint32_t n_big;          // candidates above the big-candidate split (listed in FrameDesc::big)
     uint32_t span_hist[256];
     uint32_t mean_hist[64];
     uint32_t bin_base[64];   // first flattened position of each area bin
@@ -94,6 +95,8 @@ struct FrameDesc {
                                    // starts a shared-memory segment (band-local unions done)
     uint32_t* band_bins;           // tile_h * 64 candidate counts, then exclusive prefixes
     uint32_t* candidates;          // max_candidates root slots, canonical order
+    uint32_t* big;                 // max_candidates: positions in `candidates` of those whose bbox
+                                   // side exceeds the split (n_big of them, any order)
     FrameState* state;
     float* hull_quads;             // max_candidates * 8
     float* quads;                  // 2 * max_candidates * 8 (per family)

@@ -334,7 +334,7 @@ def measure_mixed_batches(steps: int, streams: int = 4, pool_batches: int = 8):
             "tuned_batch_gpu_ms": round(tuned_ms, 4), "bit_exact_vs_single_frame": bool(exact)}
 
 
-def measure_serving(seconds: float, pool_per_cam: int = 12):
+def measure_serving(seconds: float, pool_per_cam: int = 12, peaks=None):
     """Six camera streams (Poisson arrivals at 60-120 fps each, sizes from
     640x480 to 3840x2160): continuous batching through bd_server versus a FIFO plain
     per-frame detector fed by the same arrivals."""
@@ -359,6 +359,7 @@ def measure_serving(seconds: float, pool_per_cam: int = 12):
     tickets: list = []
     lat: list[float] = []
     dropped = [0]
+    accepted: list[int] = []  # camera of every admitted frame
     done = threading.Event()
 
     def collector():
@@ -383,9 +384,11 @@ def measure_serving(seconds: float, pool_per_cam: int = 12):
             dropped[0] += 1
         else:
             tickets.append(tk)
+            accepted.append(c)
     done.set()
     th.join()
     wall = time.perf_counter() - t0
+    served_bytes = sum(cams[c][0] * cams[c][1] for c in accepted)
     st = server.stats()
     server.close()
     serve = {"frames_per_s": round(len(lat) / wall, 2), "p50_ms": round(pct(lat, 50), 4),
@@ -393,7 +396,11 @@ def measure_serving(seconds: float, pool_per_cam: int = 12):
              "offered_fps": round(len(arrivals) / seconds, 2), "seconds": seconds,
              "batches": int(st.batches), "mean_batch_frames": round(st.mean_batch_frames, 3),
              "plans": int(st.plans), "peak_inflight": int(st.peak_inflight),
-             "device_bytes": int(st.device_bytes)}
+             "device_bytes": int(st.device_bytes),
+             # frame bytes served per second against the measured HBM copy peak
+             "frame_gbs": round(served_bytes / wall / 1e9, 4),
+             "hbm_frac": (round(served_bytes / wall / 1e9 / peaks["hbm_gbs"], 7)
+                          if peaks and peaks.get("hbm_gbs") else None)}
     # Plain per-frame detect on the same arrivals: measured service time per
     # (camera, frame) -- both families -- fed through a FIFO queue.
     dets = [[bdcudatag.Detector(f, w, h) for f in (0, 1)] for w, h, _, _ in cams]
@@ -646,7 +653,7 @@ def bench_ours(args, rank, world, local_rank):
     roof = measure_roofline(plans[0], sets_dev, peaks)
     plain = measure_plain(frames, args.plain_frames)
     cpu = measure_cpu_baseline(frames)
-    serving = measure_serving(args.serving_seconds) if args.serving_seconds > 0 else None
+    serving = measure_serving(args.serving_seconds, peaks=peaks) if args.serving_seconds > 0 else None
     refine = measure_refine()
     mixed = measure_mixed_batches(max(200, args.steps // 5), streams=args.streams)
     result_bytes = BATCH * ((32 + 2 * plans[0].max_detections * 84 + 255) // 256 * 256)
