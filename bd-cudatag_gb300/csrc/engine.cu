@@ -228,7 +228,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     std::vector<size_t> off_frame(nf), off_tmin(nf), off_tmax(nf), off_lo(nf), off_hi(nf),
         off_bits(nf), off_rc(nf), off_runs(nf), off_parent(nf), off_area(nf), off_bbox(nf),
         off_meta(nf), off_bands(nf), off_cands(nf), off_hull(nf), off_quads(nf), off_dec(nf),
-        off_lroots(nf), off_lcount(nf), off_mode(nf), off_dech(nf), off_big(nf);
+        off_lroots(nf), off_lcount(nf), off_mode(nf), off_dech(nf), off_fit(nf);
     im.frame_offset.resize(nf);
     size_t frame_total = 0;
     for (int i = 0; i < nf; ++i) {
@@ -286,7 +286,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
         off_mode[i] = carve.take(sizeof(uint32_t) * d.tile_h);
         off_bands[i] = carve.take(sizeof(uint32_t) * 64 * d.tile_h);
         off_cands[i] = carve.take(sizeof(uint32_t) * mc);
-        off_big[i] = carve.take(sizeof(uint32_t) * mc);
+        off_fit[i] = carve.take(sizeof(uint32_t) * mc);
         off_hull[i] = carve.take(sizeof(float) * 8 * mc);
         off_quads[i] = carve.take(sizeof(float) * 16 * mc);
         off_dec[i] = carve.take(sizeof(DecodeOut) * 2 * mc);
@@ -328,7 +328,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
         d.band_mode = reinterpret_cast<uint32_t*>(base + off_mode[i]);
         d.band_bins = reinterpret_cast<uint32_t*>(base + off_bands[i]);
         d.candidates = reinterpret_cast<uint32_t*>(base + off_cands[i]);
-        d.big = reinterpret_cast<uint32_t*>(base + off_big[i]);
+        d.fit_list = reinterpret_cast<uint32_t*>(base + off_fit[i]);
         d.state = im.states + i;
         d.hull_quads = reinterpret_cast<float*>(base + off_hull[i]);
         d.quads = reinterpret_cast<float*>(base + off_quads[i]);

@@ -192,14 +192,14 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
         cudaStreamWaitEvent(s2, static_cast<cudaEvent_t>(fork->fork_event), 0);
         k_fit_decode_big<<<big_grid, 256, 0, s2>>>(dd, io, split);
         cudaEventRecord(static_cast<cudaEvent_t>(fork->join_event), s2);
-        k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io, split);
+        k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io);
         cudaStreamWaitEvent(s, static_cast<cudaEvent_t>(fork->join_event), 0);
         mark(6);
         mark(7);
     } else {
         if (split > 0) k_fit_decode_big<<<big_grid, 256, 0, s>>>(dd, io, split);
         mark(6);
-        k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io, split);
+        k_fit_decode<<<quad_grid, warps * 32, quad_smem, s>>>(dd, io);
         mark(7);
     }
     k_finalize<<<hd.frames * 2, kFinalThreads, 0, s>>>(dd);

@@ -541,8 +541,8 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
 
         // Components by hooking and flattening rounds.  A round hooks, for
         // every overlapping pair with different parents, the larger parent
-        // under the smaller one (atomicMin), then flattens the forest by
-        // pointer jumping, so every round starts from roots.  Parents only
+        // under the smaller one (atomicMin), then flattens the forest, so
+        // every round starts from roots.  Parents only
         // decrease and always stay in the component, so the rounds end; the
         // last one finds every pair under one root, which is the component's
         // smallest index, as with the reference's union-find.  Each round
@@ -563,18 +563,15 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
                 }
             }
             if (!__syncthreads_or(hooked)) break;
-            for (;;) {
-                int changed = 0;
-                for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
-                    const uint32_t p = sm_par[i];
-                    const uint32_t gp = sm_par[p];
-                    if (gp != p) {
-                        sm_par[i] = gp;
-                        changed = 1;
-                    }
-                }
-                if (!__syncthreads_or(changed)) break;
+            // Flatten in one pass: every entry walks to its root.  No hook
+            // runs meanwhile, and a concurrent write only ever shortcuts a
+            // walk to an ancestor.
+            for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
+                uint32_t r = sm_par[i];
+                for (uint32_t q = sm_par[r]; q != r; q = sm_par[r]) r = q;
+                sm_par[i] = r;
             }
+            __syncthreads();
         }
         for (uint32_t i = tid; i < seg_n; i += blockDim.x) sm_area[i] = 0u;
         __syncthreads();
@@ -803,7 +800,7 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     __shared__ uint32_t s_base[64];
     __shared__ uint32_t s_cprefix[kMaxBandsPerFrame + 1];  // candidates before each band
     __shared__ uint32_t s_warp_sum[8];
-    __shared__ uint32_t s_ncand, s_limit, s_nbig;
+    __shared__ uint32_t s_ncand, s_limit, s_nbig, s_nsmall;
     __shared__ int s_last;
 
     const int tid = threadIdx.x;
@@ -910,6 +907,7 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
         s_limit = min(pos, static_cast<uint32_t>(d.max_candidates));
         st->n_candidates = s_limit;
         s_nbig = 0;
+        s_nsmall = 0;
     }
 
     // Placement (reference k_order_candidates :642-654): candidate j of the
@@ -949,15 +947,21 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
         const uint32_t pos = s_base[cbin] + __ldcg(&d.band_bins[lo * 64 + cbin]) + (meta & 0xffffffu);
         if (pos < limit) {
             d.candidates[pos] = slot;
-            // The CTA path's work list: big candidates, listed once here
-            // instead of found by every CTA of k_fit_decode_big.
+            // The fit/decode work lists, split by size once here: big
+            // candidates (a CTA each) from the front, the others (a warp
+            // per family) from the back.
             if (big_candidate(reinterpret_cast<const uint4*>(d.bbox)[slot], split_px)) {
-                d.big[atomicAdd(&s_nbig, 1u)] = pos;
+                d.fit_list[atomicAdd(&s_nbig, 1u)] = pos;
+            } else {
+                d.fit_list[d.max_candidates - 1 - static_cast<int>(atomicAdd(&s_nsmall, 1u))] = pos;
             }
         }
     }
     __syncthreads();
-    if (tid == 0) st->n_big = s_nbig;
+    if (tid == 0) {
+        st->n_big = s_nbig;
+        st->n_small = s_nsmall;
+    }
 }
 
 }  // namespace bdgb

@@ -858,14 +858,15 @@ __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uin
                                   int64_t stride, bool quad_ok, int lane, const float* cell_uv,
                                   QuadSmem& sm);
 
-// Flattened work list of (frame, candidate, family) items, the families of
-// a candidate adjacent; warp w of CTA c takes items c * warps + w, then
-// strides by grid * warps.  Each warp builds the candidate's hull itself (the
+// Flattened work list of (frame, candidate, family) items over the
+// candidates at or below the big-candidate split (the back of
+// FrameDesc::fit_list), the families of a candidate adjacent; warp w of CTA
+// c takes items c * warps + w, then strides by grid * warps.  Each warp builds the candidate's hull itself (the
 // warp of the frame's lowest family also stores it), so the families of a
 // candidate proceed concurrently and warps never wait for one another after
 // the work-list prefix.
 __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict__ b,
-                                                    const FrameIO* __restrict__ io, int split_px) {
+                                                    const FrameIO* __restrict__ io) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
     __shared__ int s_prefix[kMaxFrames + 1];
     __shared__ float s_uv[2][8];
@@ -880,7 +881,7 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
         int run = 0;
         for (int f = 0; f < b->frames; ++f) {
             s_prefix[f] = run;
-            run += static_cast<int>(b->f[f].state->n_candidates) * __popc(b->f[f].families & 3u);
+            run += static_cast<int>(b->f[f].state->n_small) * __popc(b->f[f].families & 3u);
         }
         s_prefix[b->frames] = run;
     }
@@ -902,15 +903,15 @@ __global__ void __launch_bounds__(256) k_fit_decode(const BatchDesc* __restrict_
         const uint32_t fams = d.families & 3u;
         const int nfam = __popc(fams);
         const int local = item - s_prefix[fi];
-        const int ci = local / nfam;
-        const int slot = local - ci * nfam;
+        const int k = local / nfam;
+        const int slot = local - k * nfam;
+        const int ci = static_cast<int>(d.fit_list[d.max_candidates - 1 - k]);
         const int fam = (slot == 0 && (fams & 1u)) ? 0 : 1;
         const bool first_family = slot == 0;
         const uint8_t* __restrict__ gray = io[fi].gray;
         const int64_t stride = io[fi].stride;
         const uint32_t root = d.candidates[ci];
         const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[root];
-        if (big_candidate(bb, split_px)) continue;  // k_fit_decode_big's
         const int x0 = static_cast<int>(bb.x), y0 = static_cast<int>(bb.y);
         const int x1 = static_cast<int>(bb.z), y1 = static_cast<int>(bb.w);
         const int rows = y1 - y0 + 1;
@@ -1051,7 +1052,7 @@ __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uin
 // group per edge), and warps 2s / 2s+1 decode the refined / hull quad of
 // slot s (the hull result is used only when no refined rotation decodes).
 // CTA c takes big candidates c, c + grid, ... of the lists k_cand_count
-// wrote (FrameDesc::big).
+// wrote (the front of FrameDesc::fit_list).
 __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __restrict__ b,
                                                         const FrameIO* __restrict__ io, int split_px) {
     constexpr int kWarps = 8;
@@ -1103,7 +1104,7 @@ __global__ void __launch_bounds__(256, 3) k_fit_decode_big(const BatchDesc* __re
             int fi = 0;
             while (s_prefix[fi + 1] <= item) ++fi;
             const FrameDesc& d = b->f[fi];
-            const int ci = static_cast<int>(d.big[item - s_prefix[fi]]);
+            const int ci = static_cast<int>(d.fit_list[item - s_prefix[fi]]);
             const int mc = d.max_candidates;
             const uint8_t* __restrict__ gray = io[fi].gray;
             const int64_t stride = io[fi].stride;

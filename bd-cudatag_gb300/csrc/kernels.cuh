@@ -48,7 +48,7 @@ __global__ void k_binarize_runs(const BatchDesc* b, const FrameIO* io, int cap, 
 __global__ void k_merge(const BatchDesc* b, const FrameIO* io, int row_cap_max);
 __global__ void k_region_stats(const BatchDesc* b, const FrameIO* io);
 __global__ void k_cand_count(const BatchDesc* b, const FrameIO* io, int split_px);
-__global__ void k_fit_decode(const BatchDesc* b, const FrameIO* io, int split_px);
+__global__ void k_fit_decode(const BatchDesc* b, const FrameIO* io);
 __global__ void k_fit_decode_big(const BatchDesc* b, const FrameIO* io, int split_px);
 __global__ void k_finalize(const BatchDesc* b);
 

@@ -41,7 +41,8 @@ struct FrameState {
     uint32_t done_stats;     // CTAs of the stats stage finished
     uint32_t done_cands;     // CTAs of the candidate-count stage finished
     uint32_t n_candidates;   // min(counts[0], max_candidates)
-    uint32_t n_big;          // candidates above the big-candidate split (listed in FrameDesc::big)
+    uint32_t n_big;          // candidates above the big-candidate split (front of FrameDesc::fit_list)
+    uint32_t n_small;        // the others (back of FrameDesc::fit_list)
     uint32_t span_hist[256];
     uint32_t mean_hist[64];
     uint32_t bin_base[64];   // first flattened position of each area bin
@@ -95,8 +96,9 @@ struct FrameDesc {
                                    // starts a shared-memory segment (band-local unions done)
     uint32_t* band_bins;           // tile_h * 64 candidate counts, then exclusive prefixes
     uint32_t* candidates;          // max_candidates root slots, canonical order
-    uint32_t* big;                 // max_candidates: positions in `candidates` of those whose bbox
-                                   // side exceeds the split (n_big of them, any order)
+    uint32_t* fit_list;            // max_candidates positions in `candidates`: from the front the
+                                   // n_big whose bbox side exceeds the split (k_fit_decode_big),
+                                   // from the back the n_small others (k_fit_decode); any order
     FrameState* state;
     float* hull_quads;             // max_candidates * 8
     float* quads;                  // 2 * max_candidates * 8 (per family)
