@@ -763,10 +763,12 @@ __global__ void __launch_bounds__(256) k_region_stats(const BatchDesc* __restric
 //    ascending root id inside a bin; the reference orders a bin by atomicAdd
 //    arrival (k_collect_candidates :591-638).
 // ===========================================================================
-__device__ __forceinline__ int candidate_bin(const FrameDesc& d, uint32_t idx) {
+__device__ __forceinline__ int candidate_bin(const FrameDesc& d, uint32_t idx, int split_px,
+                                             bool* big) {
     const int a = static_cast<int>(d.area[idx]);
-    if (a < d.min_cluster_pixels) return -1;
     const uint4 bb = reinterpret_cast<const uint4*>(d.bbox)[idx];
+    *big = big_candidate(bb, split_px);
+    if (a < d.min_cluster_pixels) return -1;
     const int x0 = static_cast<int>(bb.x), y0 = static_cast<int>(bb.y);
     const int x1 = static_cast<int>(bb.z), y1 = static_cast<int>(bb.w);
     const int bw = x1 - x0 + 1;
@@ -830,12 +832,16 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         const uint32_t i = base + tid;
         int bin = -1;
+        bool big = false;
         uint32_t slot = 0;
         if (i < total) {
             slot = band_slot(s_rowoff, y0, row_cap, i);
-            const uint32_t root = uf_root_readonly(d.parent, slot);
+            // Two hops reach the root: a run's parent is a band root (or a
+            // root above it after k_merge's path halving), and k_region_stats
+            // pointed every band root at its component's root.
+            const uint32_t root = __ldcg(d.parent + __ldcg(d.parent + slot));
             d.parent[slot] = root;
-            if (root == slot) bin = candidate_bin(d, slot);
+            if (root == slot) bin = candidate_bin(d, slot, split_px, &big);
         }
         const uint32_t key = bin >= 0 ? static_cast<uint32_t>(bin) : 64u + lane;
         const uint32_t peers = __match_any_sync(kFull, key);
@@ -849,7 +855,7 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
         if (bin >= 0) {
             uint32_t pos = s_run[bin] + rank;
             for (int w2 = 0; w2 < w; ++w2) pos += s_wbin[w2][bin];
-            meta = (static_cast<uint32_t>(bin) << 24) | pos;
+            meta = (static_cast<uint32_t>(bin) << 24) | (big ? 1u << 23 : 0u) | pos;
         }
         __syncthreads();
         if (tid < 64) {
@@ -944,13 +950,13 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
         const uint32_t slot = __ldcg(&d.lroots[static_cast<int64_t>(lo) * kTile * row_cap + (j - s_cprefix[lo])]);
         const uint32_t meta = __ldcg(&d.cand_meta[slot]);
         const uint32_t cbin = meta >> 24;
-        const uint32_t pos = s_base[cbin] + __ldcg(&d.band_bins[lo * 64 + cbin]) + (meta & 0xffffffu);
+        const uint32_t pos = s_base[cbin] + __ldcg(&d.band_bins[lo * 64 + cbin]) + (meta & 0x7fffffu);
         if (pos < limit) {
             d.candidates[pos] = slot;
             // The fit/decode work lists, split by size once here: big
             // candidates (a CTA each) from the front, the others (a warp
             // per family) from the back.
-            if (big_candidate(reinterpret_cast<const uint4*>(d.bbox)[slot], split_px)) {
+            if (meta & (1u << 23)) {
                 d.fit_list[atomicAdd(&s_nbig, 1u)] = pos;
             } else {
                 d.fit_list[d.max_candidates - 1 - static_cast<int>(atomicAdd(&s_nsmall, 1u))] = pos;

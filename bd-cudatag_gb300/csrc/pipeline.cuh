@@ -89,7 +89,7 @@ struct FrameDesc {
     uint32_t* parent;              // slots: union-find, then the root of every run
     uint32_t* area;                // slots (valid at roots)
     uint32_t* bbox;                // 4 * slots (valid at roots)
-    uint32_t* cand_meta;           // slots: bin << 24 | rank in band, or kNone
+    uint32_t* cand_meta;           // slots: bin << 24 | big << 23 | rank in band, or kNone
     uint32_t* lroots;              // slots: per band (at its first slot) the band-local roots
     uint32_t* lroot_count;         // tile_h: band-local roots per band
     uint32_t* band_mode;           // tile_h: bit 0 fallback (one root per run), else bit r: row r
