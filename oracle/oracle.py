@@ -15,7 +15,10 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "liboracle.so"
-_LIB = None
+# The same restatement built with multiply-add contraction (as nvcc builds the
+# reference): only the rounding-sensitivity test uses it.
+LIB_FMA_PATH = HERE / "_build" / "liboracle_fma.so"
+_LIBS: dict = {}
 
 
 class Config(ctypes.Structure):
@@ -63,12 +66,12 @@ def build() -> Path:
     return LIB_PATH
 
 
-def lib() -> ctypes.CDLL:
-    global _LIB
-    if _LIB is None:
-        if not LIB_PATH.exists():
+def lib(fma: bool = False) -> ctypes.CDLL:
+    if fma not in _LIBS:
+        path = LIB_FMA_PATH if fma else LIB_PATH
+        if not path.exists():
             build()
-        L = ctypes.CDLL(str(LIB_PATH))
+        L = ctypes.CDLL(str(path))
         L.bdo_run.restype = ctypes.c_void_p
         L.bdo_run.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                               ctypes.c_int32, ctypes.POINTER(Config)]
@@ -91,8 +94,8 @@ def lib() -> ctypes.CDLL:
             getattr(L, name).restype = ctypes.c_float
         L.bdo_atan2f.argtypes = [ctypes.c_float, ctypes.c_float]
         L.bdo_atan2f.restype = ctypes.c_float
-        _LIB = L
-    return _LIB
+        _LIBS[fma] = L
+    return _LIBS[fma]
 
 
 _STAGE_DTYPES = {
@@ -109,7 +112,7 @@ class Frame:
     """One frame run through the oracle; stage buffers on demand."""
 
     def __init__(self, gray: np.ndarray, family: int = 0, config: Config | None = None,
-                 stride: int | None = None):
+                 stride: int | None = None, fma: bool = False):
         gray = np.ascontiguousarray(gray, dtype=np.uint8) if stride is None else gray
         h, w = gray.shape[0], (gray.shape[1] if stride is None else None)
         if stride is None:
@@ -118,29 +121,30 @@ class Frame:
             w = gray.shape[1] if w is None else w
         self.width, self.height, self.family = int(w), int(h), family
         cfg = config if config is not None else default_config()
-        self._h = lib().bdo_run(gray.ctypes.data, self.width, self.height, stride, family,
+        self._lib = lib(fma)
+        self._h = self._lib.bdo_run(gray.ctypes.data, self.width, self.height, stride, family,
                                 ctypes.byref(cfg))
         if not self._h:
             raise ValueError("oracle rejected the frame")
         g = (ctypes.c_int32 * 9)()
-        lib().bdo_geometry(self._h, g)
+        self._lib.bdo_geometry(self._h, g)
         (self.tile_w, self.tile_h, self.words, self.row_cap, self.max_candidates,
          self.max_detections, self.dim, self.max_hamming, self.candidate_count) = list(g)
 
     def __del__(self):
         if getattr(self, "_h", None):
-            lib().bdo_free(self._h)
+            self._lib.bdo_free(self._h)
             self._h = None
 
     def detections(self, capacity: int | None = None) -> tuple[int, np.ndarray]:
         cap = self.max_detections if capacity is None else capacity
         out = np.zeros(max(cap, 1), dtype=DETECTION_DTYPE)
-        found = lib().bdo_detections(self._h, out.ctypes.data, cap)
+        found = self._lib.bdo_detections(self._h, out.ctypes.data, cap)
         return found, out[:min(found, cap)]
 
     def counts(self) -> np.ndarray:
         c = np.zeros(5, dtype=np.uint32)
-        lib().bdo_counts(self._h, c.ctypes.data)
+        self._lib.bdo_counts(self._h, c.ctypes.data)
         return c
 
     def refit64(self, gray: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
@@ -152,16 +156,16 @@ class Frame:
         q = np.full((max(n, 1), 8), np.nan)
         img = np.ascontiguousarray(gray, dtype=np.uint8)
         assert img.shape == (self.height, self.width)
-        lib().bdo_refit64(self._h, img.ctypes.data, hq.ctypes.data, q.ctypes.data)
+        self._lib.bdo_refit64(self._h, img.ctypes.data, hq.ctypes.data, q.ctypes.data)
         return hq[:n], q[:n]
 
     def stage(self, name: str) -> np.ndarray:
-        size = lib().bdo_stage(self._h, name.encode(), None, 0)
+        size = self._lib.bdo_stage(self._h, name.encode(), None, 0)
         if size < 0:
             raise KeyError(name)
         dt = np.dtype(_STAGE_DTYPES[name])
         out = np.zeros(size // dt.itemsize, dtype=dt)
-        lib().bdo_stage(self._h, name.encode(), out.ctypes.data, size)
+        self._lib.bdo_stage(self._h, name.encode(), out.ctypes.data, size)
         return out
 
 
