@@ -364,3 +364,34 @@ def test_gpu_corners_against_fp64_refit():
     assert np.median(err[same]) < 5e-3 and err[same].max() < 0.1
     assert np.mean(err > 0.1) <= 0.05
     assert np.nanmedian(rel[same]) < 1e-4
+
+
+@pytest.mark.parametrize("split", [0, 32, 48, 96])
+def test_fit_work_lists_split_candidates_by_size(split):
+    """k_cand_count's placing CTA lists the candidates above the split (for
+    the CTA path) and the rest (for the warp path); every candidate is on
+    exactly one list, and the results do not depend on the split."""
+    torch = pytest.importorskip("torch")
+    sizes = [(1280, 800), (640, 480), (1920, 1080)]
+    frames = [scenes.render_scene(scenes.MIXED_1280, 5, 1280, 800)[0],
+              scenes.render_scene(scenes.EIGHT_TAGS_640, 3, 640, 480)[0],
+              scenes.render_scene(scenes.MULTI_SIZE, 9, 1920, 1080)[0]]
+    batch = bdcudatag.Batch([(w, h, 3) for w, h in sizes])
+    batch.set_launch(quad_split=split)
+    found, out = batch.detect([torch.from_numpy(f).cuda() for f in frames], [w for w, _ in sizes],
+                              device=True)
+    for i, img in enumerate(frames):
+        ref = oracle.Frame(img, 0)
+        nc = min(ref.candidate_count, ref.max_candidates)
+        state = batch.stage(i, "state")
+        # FrameState: counts[5], top_enc, bottom_enc, ref[2], done_stats,
+        # done_cands, n_candidates, n_big, n_small, ...
+        n_candidates, n_big, n_small = int(state[11]), int(state[12]), int(state[13])
+        assert n_candidates == nc and n_big + n_small == nc
+        bb = ref.stage("bbox").reshape(-1, 4)[ref.stage("candidates")[:nc]].astype(np.int64)
+        side = np.maximum(bb[:, 2] - bb[:, 0], bb[:, 3] - bb[:, 1]) + 1
+        assert n_big == (int(np.sum(side > split)) if split > 0 else 0)
+        for fam in (0, 1):
+            wn, want = oracle.Frame(img, fam).detections()
+            assert found[i, fam] == wn
+            same_records(out[i, fam, :wn], want)
