@@ -377,8 +377,14 @@ def measure_serving(seconds: float, pool_per_cam: int = 12, peaks=None):
     th.start()
     t0 = time.perf_counter()
     for t, c, k in arrivals:
-        while time.perf_counter() - t0 < t:
-            pass
+        # Sleep (which lets the collector thread run) until just before the
+        # arrival, then spin for the last fraction of a millisecond.
+        while True:
+            ahead = t - (time.perf_counter() - t0)
+            if ahead <= 0:
+                break
+            if ahead > 5e-4:
+                time.sleep(ahead - 3e-4)
         tk = server.submit(c, pools[c][1][k % pool_per_cam])
         if tk < 0:
             dropped[0] += 1
