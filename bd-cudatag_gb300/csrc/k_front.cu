@@ -225,10 +225,10 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
 //    The runs of a band are labelled in shared memory (same-row fragments and
 //    8-connected runs of consecutive rows inside the band, by hooking and
 //    flattening rounds), and area / bbox are aggregated per band-local root
-//    with shared-memory atomics.  Global
-//    memory then receives one parent link per run (to its band-local root)
-//    and one aggregate per band-local root; k_merge only unions across band
-//    boundaries and k_region_stats folds band roots into global roots.  The
+//    with shared-memory atomics.  Global memory then receives one parent
+//    link per run (to its band-local root) and one aggregate per band-local
+//    root; k_merge only unions across band boundaries and k_region_stats
+//    folds band roots into global roots.  The
 //    local root is the band's smallest slot of the component, so every root
 //    is still the component's smallest slot id (reference invariant,
 //    gpu_detector.cu:398-421).  A band with more than `cap` runs (a launch
@@ -542,13 +542,12 @@ __global__ void __launch_bounds__(256) k_binarize_runs(const BatchDesc* __restri
         // Components by hooking and flattening rounds.  A round hooks, for
         // every overlapping pair with different parents, the larger parent
         // under the smaller one (atomicMin), then flattens the forest, so
-        // every round starts from roots.  Parents only
-        // decrease and always stay in the component, so the rounds end; the
-        // last one finds every pair under one root, which is the component's
-        // smallest index, as with the reference's union-find.  Each round
-        // merges every tree with a neighbour: 3-5 rounds on 8-row bands of
-        // camera frames, where concurrent union-find walked chains of
-        // hundreds of links.
+        // every round starts from roots.  Parents only decrease and always
+        // stay in the component, so the rounds end; the last one finds every
+        // pair under one root, which is the component's smallest index, as
+        // with the reference's union-find.  Each round merges every tree with
+        // a neighbour: 3-5 rounds on 8-row bands of camera frames, where
+        // concurrent union-find walked chains of hundreds of links.
         for (;;) {
             int hooked = 0;
             for (uint32_t i = tid; i < seg_n; i += blockDim.x) {
