@@ -561,7 +561,9 @@ def bench_reference(args, rank):
         return
     frames, _ = render_pool(64)
     cores = os.cpu_count() or 1
-    step_frames = BATCH
+    # A step is a bounded sample that keeps every host thread busy: one
+    # (frame, family) task per thread, in whole 4-camera batches.
+    step_frames = max(BATCH, (cores // 2 + BATCH - 1) // BATCH * BATCH)
     for k in range(args.warmup):
         oracle.detect_many(frames[(k * step_frames) % 64:][:step_frames], [FAMILIES] * step_frames,
                            threads=cores)
@@ -580,7 +582,8 @@ def bench_reference(args, rank):
         "ms_per_step": round(total * 1e3 / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "p50_ms": pct(times, 50), "p99_ms": pct(times, 99),
-        "config": {"workload": WORKLOAD, "batch_frames": step_frames, "frames_pool": 64},
+        "config": {"workload": WORKLOAD, "batch_frames": BATCH, "frames_per_step": step_frames,
+                   "frames_pool": 64},
         "cpu_baseline": {"value": round(value, 2), "unit": "frames/s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} steps of {step_frames} 1280x800 workload frames (both "
                                    f"families) from 64 seeded frames"},

@@ -1292,27 +1292,29 @@ int32_t bdo_detect_many(int32_t frames, const uint8_t* const* grays, const int32
         !counts || max_detections < 1) {
         return -1;
     }
+    // Work units are (frame, family) pairs, so a few frames still keep every
+    // thread busy.
     std::atomic<int32_t> next{0};
     const int nthreads = std::max(1, threads);
     auto worker = [&]() {
         for (;;) {
-            const int32_t i = next.fetch_add(1);
-            if (i >= frames) return;
-            for (int fam = 0; fam < 2; ++fam) {
-                int32_t* count = &counts[i * 2 + fam];
-                bd_detection* dst = out + (static_cast<size_t>(i) * 2 + fam) * max_detections;
-                if (!(family_masks[i] & (1u << fam))) {
-                    *count = -1;
-                    continue;
-                }
-                bdo_frame* f = bdo_run(grays[i], widths[i], heights[i], strides[i], fam, config);
-                if (!f) {
-                    *count = -1;
-                    continue;
-                }
-                *count = bdo_detections(f, dst, max_detections);
-                bdo_free(f);
+            const int32_t unit = next.fetch_add(1);
+            if (unit >= 2 * frames) return;
+            const int32_t i = unit >> 1;
+            const int fam = unit & 1;
+            int32_t* count = &counts[i * 2 + fam];
+            bd_detection* dst = out + (static_cast<size_t>(i) * 2 + fam) * max_detections;
+            if (!(family_masks[i] & (1u << fam))) {
+                *count = -1;
+                continue;
             }
+            bdo_frame* f = bdo_run(grays[i], widths[i], heights[i], strides[i], fam, config);
+            if (!f) {
+                *count = -1;
+                continue;
+            }
+            *count = bdo_detections(f, dst, max_detections);
+            bdo_free(f);
         }
     };
     std::vector<std::thread> pool;

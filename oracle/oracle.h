@@ -65,8 +65,8 @@ void bdo_geometry(const bdo_frame* frame, int32_t out[9]);
 //  corners; id -1 when nothing decoded).
 int64_t bdo_stage(const bdo_frame* frame, const char* name, void* dst, int64_t dst_bytes);
 
-// Detects every frame of a set on `threads` host threads (frame-parallel),
-// one family per family bit.  out holds frames*2 blocks of max_detections
+// Detects every frame of a set on `threads` host threads, one (frame,
+// family) pair per task, one family per family bit.  out holds frames*2 blocks of max_detections
 // records; counts[frame*2+family] = found (or -1 if that family was not
 // requested).  Returns 0 on success.
 int32_t bdo_detect_many(int32_t frames, const uint8_t* const* grays, const int32_t* widths,
