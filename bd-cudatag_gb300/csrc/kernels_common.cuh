@@ -79,7 +79,8 @@ __device__ __forceinline__ void uf_union(uint32_t* parent, uint32_t a, uint32_t 
             b = t;
         }
         const uint32_t old = atomicMin(&parent[b], a);
-        if (old == a) break;
+        // b was still a root (now under a), or already under a: joined.
+        if (old == b || old == a) break;
         b = uf_find(parent, old);
     }
 }
