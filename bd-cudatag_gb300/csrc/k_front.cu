@@ -646,7 +646,7 @@ __device__ __forceinline__ void merge_run_with_row_above(uint32_t* parent, const
     }
 }
 
-__global__ void __launch_bounds__(256) k_merge(const BatchDesc* __restrict__ b,
+__global__ void __launch_bounds__(256, 2) k_merge(const BatchDesc* __restrict__ b,
                                                const FrameIO* __restrict__ io, int row_cap_max) {
     const int fi = frame_of_band(b, blockIdx.x);
     if (!io[fi].gray) return;  // slot not used in this launch

@@ -69,9 +69,31 @@ __device__ __forceinline__ uint32_t uf_root_readonly(const uint32_t* parent, uin
     }
 }
 
+// Roots of *a and *b, the two chains walked in lockstep (path halving on
+// both, as uf_find) so that their loads are in flight together.
+__device__ __forceinline__ void uf_find2(uint32_t* parent, uint32_t* a, uint32_t* b) {
+    uint32_t x = *a, y = *b;
+    for (;;) {
+        const uint32_t px = parent[x], py = parent[y];
+        const bool rx = px == x, ry = py == y;
+        if (rx && ry) break;
+        const uint32_t gx = rx ? px : parent[px];
+        const uint32_t gy = ry ? py : parent[py];
+        if (!rx) {
+            parent[x] = gx;
+            x = gx;
+        }
+        if (!ry) {
+            parent[y] = gy;
+            y = gy;
+        }
+    }
+    *a = x;
+    *b = y;
+}
+
 __device__ __forceinline__ void uf_union(uint32_t* parent, uint32_t a, uint32_t b) {
-    a = uf_find(parent, a);
-    b = uf_find(parent, b);
+    uf_find2(parent, &a, &b);
     while (a != b) {
         if (a > b) {
             const uint32_t t = a;
