@@ -395,3 +395,53 @@ def test_fit_work_lists_split_candidates_by_size(split):
             wn, want = oracle.Frame(img, fam).detections()
             assert found[i, fam] == wn
             same_records(out[i, fam, :wn], want)
+
+
+def _ccl_patterns():
+    """Binary-ish frames that stress connected-component labelling: a comb
+    (many bars joined only at the top), a zigzag snake crossing every band,
+    a checkerboard (8-connected diagonal joins only), and noise of several
+    densities."""
+    h, w = 240, 512
+    comb = np.full((h, w), 220, np.uint8)
+    comb[20:200, 40:480:6] = 30
+    comb[20:24, 40:480] = 30
+    snake = np.full((h, w), 220, np.uint8)
+    for k, y in enumerate(range(10, 230, 6)):
+        snake[y:y + 3, 20:490] = 30
+        x = 487 if k % 2 == 0 else 20
+        snake[y:y + 9, x:x + 3] = 30
+    board = np.full((h, w), 220, np.uint8)
+    yy, xx = np.mgrid[0:h, 0:w]
+    board[((yy // 2) + (xx // 2)) % 2 == 0] = 30
+    board[:8], board[-8:], board[:, :8], board[:, -8:] = 220, 220, 220, 220
+    rng = np.random.default_rng(5)
+    noise = [np.where(rng.random((h, w)) < p, 30, 220).astype(np.uint8) for p in (0.3, 0.5, 0.6)]
+    return [comb, snake, board] + noise
+
+
+@pytest.mark.parametrize("band_cap", [256, 2048])
+def test_ccl_stress_patterns(band_cap):
+    """Labels, areas and boxes bit-exact on adversarial component shapes,
+    with small (many row segments) and large shared-memory band caps."""
+    torch = pytest.importorskip("torch")
+    frames = _ccl_patterns()
+    h, w = frames[0].shape
+    batch = bdcudatag.Batch([(w, h, 1)] * len(frames))
+    batch.set_launch(band_cap=band_cap)
+    found, out = batch.detect([torch.from_numpy(f).cuda() for f in frames], [w] * len(frames),
+                              device=True)
+    for i, img in enumerate(frames):
+        ref = oracle.Frame(img, 0)
+        rc = batch.stage(i, "row_count")
+        assert np.array_equal(rc, ref.stage("row_count"))
+        valid = (np.arange(ref.row_cap)[None, :] < rc[:, None]).ravel()
+        lab = batch.stage(i, "label")[valid]
+        assert np.array_equal(lab, ref.stage("label")[valid])
+        roots = np.unique(lab)
+        assert np.array_equal(batch.stage(i, "area")[roots], ref.stage("area")[roots])
+        assert np.array_equal(batch.stage(i, "bbox").reshape(-1, 4)[roots],
+                              ref.stage("bbox").reshape(-1, 4)[roots])
+        wn, want = ref.detections()
+        assert found[i, 0] == wn
+        same_records(out[i, 0, :wn], want)
