@@ -777,14 +777,20 @@ __device__ int decode_rotations_warp(const uint8_t* __restrict__ gray, const Fra
 
 // Per-warp shared memory of k_fit_decode.
 struct QuadSmem {
-    float mags[32 * kMaxProbes];  // one probe profile per lane
+    // The probe profiles live only while edges are refined, the decode
+    // cells only while the quad is decoded: they share the space.
+    union {
+        float mags[32 * kMaxProbes];  // one probe profile per lane
+        struct {
+            float raw[4][64];         // per rotation: samples, then differences
+            float sharp[4][64];
+        } cells;
+    };
     uint32_t hull[32];
     float q[4][2];                // quad being refined
     float hq[4][2];               // hull quad
     float lines[4][4];
     int have[4];
-    float raw[4][64];             // per rotation: samples, then differences
-    float sharp[4][64];
     VariantResult res;
 };
 
@@ -1014,8 +1020,8 @@ __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uin
         // Decode: the refined quad's rotations, then the hull quad's only
         // when none of those decoded and refinement moved a corner (an
         // unmoved quad would decode the same way again).
-        int best = decode_rotations_warp(gray, d, stride, fam, &sm.q[0][0], lane, cell_uv, sm.raw,
-                                         sm.sharp, &sm.res);
+        int best = decode_rotations_warp(gray, d, stride, fam, &sm.q[0][0], lane, cell_uv, sm.cells.raw,
+                                         sm.cells.sharp, &sm.res);
         bool moved = false;
         {
             const float* qa = &sm.q[0][0];
@@ -1023,8 +1029,8 @@ __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uin
             for (int k = 0; k < 8; ++k) moved = moved || __float_as_uint(qa[k]) != __float_as_uint(qb[k]);
         }
         if (best < 0 && moved) {
-            best = decode_rotations_warp(gray, d, stride, fam, &sm.hq[0][0], lane, cell_uv, sm.raw,
-                                         sm.sharp, &sm.res);
+            best = decode_rotations_warp(gray, d, stride, fam, &sm.hq[0][0], lane, cell_uv, sm.cells.raw,
+                                         sm.cells.sharp, &sm.res);
         }
         if (lane == 0) {
             if (best < 0) {
