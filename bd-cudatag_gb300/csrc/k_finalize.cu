@@ -179,7 +179,9 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     k_region_stats<<<bands, 256, 0, s>>>(dd, io);
     mark(4);
     const int split = lc.quad_split;
-    k_cand_count<<<bands, 256, 0, s>>>(dd, io, split);
+    int th_max = 1;
+    for (int f = 0; f < hd.frames; ++f) th_max = std::max(th_max, hd.f[f].tile_h);
+    k_cand_count<<<bands, 256, (th_max + 1) * sizeof(uint32_t), s>>>(dd, io, split);
     mark(5);
     int cands = 0;
     for (int f = 0; f < hd.frames; ++f) cands += hd.f[f].max_candidates;

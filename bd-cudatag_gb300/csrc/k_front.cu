@@ -799,7 +799,9 @@ __global__ void __launch_bounds__(256) k_cand_count(const BatchDesc* __restrict_
     __shared__ uint32_t s_chunk[4][64];
     __shared__ uint32_t s_total[64];
     __shared__ uint32_t s_base[64];
-    __shared__ uint32_t s_cprefix[kMaxBandsPerFrame + 1];  // candidates before each band
+    // Candidates before each band of the frame (tallest frame's bands + 1,
+    // sized at launch).
+    extern __shared__ uint32_t s_cprefix[];
     __shared__ uint32_t s_warp_sum[8];
     __shared__ uint32_t s_ncand, s_limit, s_nbig, s_nsmall;
     __shared__ int s_last;
