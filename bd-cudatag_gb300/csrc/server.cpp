@@ -82,7 +82,8 @@ struct bd_server {
 void bd_server::finish_plan(int p) {
     bdgb::Plan& plan = *plans[p];
     std::string error;
-    if (plan.wait(&error) != 0) fatal = error;
+    const bool ok = plan.wait(&error) == 0;
+    if (!ok) fatal = error;  // every collect reports it; no result is read
     const auto now = Clock::now();
     for (size_t c = 0; c < cameras.size(); ++c) {
         const int64_t t = slot_ticket[p][c];
@@ -91,9 +92,9 @@ void bd_server::finish_plan(int p) {
         auto it = requests.find(t);
         if (it == requests.end()) continue;
         Request& r = it->second;
-        for (int f = 0; f < 2; ++f) {
+        for (int f = 0; ok && f < 2; ++f) {
             if (!((cameras[c].families >> f) & 1u)) continue;
-            const int n = std::min(plan.found(static_cast<int>(c), f), max_detections);
+            const int n = std::max(0, std::min(plan.found(static_cast<int>(c), f), max_detections));
             r.found[f] = n;
             std::memcpy(r.dets.data() + static_cast<size_t>(f) * max_detections,
                         plan.detections(static_cast<int>(c), f), sizeof(bd_detection) * n);
