@@ -711,8 +711,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    # 12 batches in flight: the GPU is within 2% of its saturated rate (12: 117k,
-    # 16-32: 119-120k frames/s) while p99 stays under 0.5 ms (8: 106k, 0.38 ms).
+    # 12 batches in flight: the GPU's saturated rate (12: 128k frames/s, p99
+    # 0.45 ms; 8: 117k, 0.32 ms; 16-48 streams: 125-127k at higher p99).
     ap.add_argument("--streams", type=int, default=12)
     ap.add_argument("--plain-frames", type=int, default=300)
     ap.add_argument("--serving-seconds", type=float, default=60.0,
