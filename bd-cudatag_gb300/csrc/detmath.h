@@ -8,8 +8,8 @@
 // with -ffp-contract=off, so the same inputs give the same bits on both.
 // That is what lets the CUDA pipeline and the CPU oracle agree bit for bit
 // on corners and decision margins.  Accuracy is about 1-2 ulp over the
-// ranges the detector uses; tests/test_detmath.py checks the error against
-// libm.
+// ranges the detector uses; tests/test_tables_and_math.py checks the error
+// against libm.
 //
 // Methods (all from the mathematics, no vendor code):
 //  * sin/cos: Cody & Waite additive range reduction by pi/2 (pi/2 split into

@@ -8,7 +8,7 @@ detector/src/tag_families.hpp:1-8).  This script reads that header in the
 reference checkout and re-emits the numbers in this project's own table
 format; it is run once, by hand, and its output is committed.
 
-    python bd-cudatag_gb300/csrc/gen_families.py /root/reference/detector/src/tag_families.hpp
+    python bd-cudatag_gb300/csrc/gen_families.py <reference checkout>/detector/src/tag_families.hpp
 """
 import re
 import sys

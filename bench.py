@@ -1,10 +1,13 @@
 """Benchmark: batched AprilTag detection on one GB300 versus plain per-frame detect.
 
-Workload (one step = one batch): 4 cameras x 1280x800 uint8 frames, both tag
-families per frame, from 600 seeded synthetic frames (6 tag36h11 + 2 tag16h5
+Workload: 4-camera batches of 1280x800 uint8 frames, both tag families per
+frame, from 600 seeded synthetic frames (6 tag36h11 + 2 tag16h5
 per frame, side 20-200 px, noise sigma 6, 3x3 blur on odd frames, two decoys
 on every fourth frame, glyph clutter past the candidate cap on every eighth).
 The 600 distinct frames (614 MB) are larger than L2, so no flush is needed.
+One step is --batches-per-step (default 32) such batches issued round-robin
+over the streams, so that even a 20-step run is long against the time it
+takes to fill and drain the streams.
 
 value     frames/s of the batched path with frames resident in HBM
           (bd_batch_submit_device), several batches in flight on S streams,
@@ -15,8 +18,10 @@ e2e       the same through the host-input C ABI (bd_batch_submit_host) with
           records inside the timed region.
 plain     the reference-style plain path: bd_detector_detect_host per frame
           and family (two detectors per frame, like two reference detectors).
-roofline  the dominant kernel's algorithmic bytes / CUDA-event duration vs
-          the measured HBM copy bandwidth.
+roofline  the pipeline's algorithmic bytes (W*H per frame, the frame read
+          once) / the timed wall, vs the measured HBM copy bandwidth; per
+          kernel the same for the two stages that stream the frame (k_stats,
+          k_binarize_runs), CUDA-event times for the latency-bound rest.
 cpu_baseline  the CPU oracle (a restatement of the reference pipeline; the
           reference has no CPU detector) on the host cores, bounded sample.
 
@@ -30,6 +35,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 from pathlib import Path
@@ -73,10 +79,11 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = REPO / "_work" / f"clocks_{os.getpid()}.csv"
+        fd, name = tempfile.mkstemp(prefix="bd_clocks_", suffix=".csv")
+        os.close(fd)
+        self.path = Path(name)
 
     def __enter__(self):
-        self.path.parent.mkdir(exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -99,6 +106,7 @@ class ClockSampler:
 
     def summary(self):
         if not self.proc or not self.path.exists():
+            self.path.unlink(missing_ok=True)
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
@@ -126,11 +134,12 @@ def barrier(world: int) -> None:
         dist.barrier()
 
 
-def aggregate_ranks(elapsed_ms: float, e2e_ms: float, steps: int, world: int, device="cuda"):
+def aggregate_ranks(elapsed_ms: float, e2e_ms: float, steps: int, world: int, device="cuda",
+                    batches_per_step: int = 1):
     """Whole-job throughput of `world` replicas: every rank processed
-    steps * BATCH frames, and the job lasts as long as the slowest rank (max
-    over ranks of the device time).  Returns (elapsed_ms, e2e_ms, value,
-    e2e_value) with the maxima."""
+    steps * batches_per_step * BATCH frames, and the job lasts as long as the
+    slowest rank (max over ranks of the device time).  Returns (elapsed_ms,
+    e2e_ms, value, e2e_value) with the maxima."""
     if world > 1:
         import torch
         import torch.distributed as dist
@@ -138,7 +147,7 @@ def aggregate_ranks(elapsed_ms: float, e2e_ms: float, steps: int, world: int, de
         t = torch.tensor([elapsed_ms, e2e_ms], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_ms, e2e_ms = float(t[0]), float(t[1])
-    frames_total = steps * BATCH * world
+    frames_total = steps * batches_per_step * BATCH * world
     return elapsed_ms, e2e_ms, frames_total / (elapsed_ms * 1e-3), frames_total / (e2e_ms * 1e-3)
 
 
@@ -224,9 +233,30 @@ def measure_plain(frames, count):
             "tag16h5 detector per frame, pageable host frames, CUDA graph"}
 
 
-def measure_roofline(plan, frame_sets, peaks):
-    """Per-stage CUDA-event times over several batches; the dominant stage's
-    algorithmic bytes per launch / its mean duration."""
+def read_traffic():
+    """Per-kernel DRAM bytes per launch (ncu dram__bytes_read.sum +
+    dram__bytes_write.sum of the 4x1280x800 batch) from the committed
+    summary, or {}."""
+    traffic = {}
+    tf = REPO / "profiles" / "dram_traffic.txt"
+    if tf.exists():
+        for line in tf.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 2 and not line.startswith("#"):
+                traffic[parts[0]] = int(parts[1])
+    return traffic
+
+
+def measure_roofline(plan, frame_sets, peaks, frames_per_s):
+    """The pipeline's roofline figure and per-stage CUDA-event times.
+
+    Pipeline: the algorithmic bytes are W*H per frame (the frame read once),
+    so achieved = frames/s * W*H over the timed wall of the batched loop.
+    Per stage: one un-graphed batch with events around every kernel
+    (bd_batch_profile_device), mean over 14 batches after 2 warm-ups.  Only
+    k_stats and k_binarize_runs stream the frame, so only they get an HBM
+    fraction (their algorithmic bytes per launch / their mean duration); the
+    other stages are gathers and union-find walks in L2, reported as time."""
     sums = None
     n = 0
     for k in range(min(16, len(frame_sets))):
@@ -237,32 +267,39 @@ def measure_roofline(plan, frame_sets, peaks):
         n += 1
     mean = {s: v / n for s, v in sums.items()}
     total = sum(mean.values())
-    dom = max(mean, key=mean.get)
     T = ((W + 7) // 8) * ((H + 7) // 8)
-    # Algorithmic bytes per frame of each HBM-facing stage.
     per_frame = {
-        "stats": W * H + 2 * T,                      # frame read once, tile min/max written
-        "binarize_runs": W * H + ((W + 31) // 32) * 4 * H,  # frame band read, bit rows written
+        "stats": W * H + 2 * T,                              # frame read once, tile min/max written
+        "binarize_runs": W * H + ((W + 31) // 32) * 4 * H,   # frame rows read, bit rows written
     }
-    stage_bytes = per_frame.get(dom, W * H) * BATCH
-    traffic = {}
-    tf = REPO / "profiles" / "dram_traffic.txt"
-    if tf.exists():
-        for line in tf.read_text().splitlines():
-            parts = line.split()
-            if len(parts) == 2 and not line.startswith("#"):
-                traffic[parts[0]] = int(parts[1])
-    achieved = stage_bytes / (mean[dom] * 1e-3) / 1e9
+    traffic = read_traffic()
     peak = peaks.get("hbm_gbs")
+    kernels = {}
+    for stage, bpf in per_frame.items():
+        if stage not in mean or mean[stage] <= 0:
+            continue
+        got = bpf * BATCH / (mean[stage] * 1e-3) / 1e9
+        kernels[f"k_{stage}"] = {
+            "bound": "hbm", "algorithmic_bytes": bpf * BATCH, "mean_launch_ms": round(mean[stage], 5),
+            "achieved": round(got, 2), "frac": round(got / peak, 5) if peak else None,
+            "traffic": traffic.get(f"k_{stage}")}
+    achieved = frames_per_s * W * H / 1e9
+    pipe_traffic = sum(traffic.values()) if traffic else None
     return {
-        "bound": "hbm", "kernel": f"k_{dom}", "achieved": round(achieved, 2), "peak": peak,
-        "unit": "GB/s", "frac": round(achieved / peak, 5) if peak else None,
+        "bound": "hbm", "kernel": "pipeline (every stage of a 4x1280x800 batch, batches in flight)",
+        "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+        "frac": round(achieved / peak, 5) if peak else None,
         "frac_of": "measured copy bandwidth (MEASURED_PEAKS.json)",
-        "bytes_per_launch": stage_bytes, "mean_launch_ms": round(mean[dom], 5),
-        "traffic": traffic.get(f"k_{dom}"),
-        "traffic_source": "ncu dram__bytes_read+write per launch, profiles/dram_traffic.txt",
+        "bytes_per_batch": W * H * BATCH,
+        "traffic": pipe_traffic,
+        "traffic_source": "sum over the batch's kernels of ncu dram__bytes_read+write per launch "
+                          "(profiles/dram_traffic.txt)",
+        "kernels": kernels,
         "stage_ms": {k: round(v, 5) for k, v in mean.items()},
+        "stage_ms_sum": round(total, 5),
         "stage_share": {k: round(v / total, 4) for k, v in mean.items()},
+        "latency_bound": "stages other than stats and binarize_runs: L2 gathers and union-find "
+                         "walks, reported as time",
     }
 
 
@@ -568,7 +605,8 @@ def bench_reference(args, rank):
     for k in range(args.warmup):
         oracle.detect_many([frames[(k * BATCH + i) % 64] for i in range(BATCH)], [FAMILIES] * BATCH,
                            threads=cores)
-    total_frames = args.steps * BATCH
+    G = args.batches_per_step
+    total_frames = args.steps * G * BATCH
     t0 = time.perf_counter()
     done = 0
     while done < total_frames:
@@ -589,9 +627,10 @@ def bench_reference(args, rank):
         "ms_per_step": round(total * 1e3 / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "p50_ms": pct(times, 50), "p99_ms": pct(times, 99),
-        "config": {"workload": WORKLOAD, "batch_frames": BATCH, "frames_pool": 64},
+        "config": {"workload": WORKLOAD, "batch_frames": BATCH, "batches_per_step": G,
+                   "step": f"{G} batches of {BATCH} frames", "frames_pool": 64},
         "cpu_baseline": {"value": round(value, 2), "unit": "frames/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} batches of {BATCH} 1280x800 workload frames (both "
+                         "sample": f"{args.steps * G} batches of {BATCH} 1280x800 workload frames (both "
                                    f"families) cycling 64 seeded frames, as (frame, family) tasks on "
                                    f"{cores} threads; p50/p99 over {len(times)} single batches"},
         "e2e": {"value": round(value, 2), "unit": "frames/s", "h2d_bytes_per_step": 0,
@@ -637,21 +676,26 @@ def bench_ours(args, rank, world, local_rank):
     elif args.tune or not args.quick:
         # Launch shapes scored on frames/s with all streams busy (untimed).
         tuned, tune_trials = tune_throughput(plans, streams, sets_dev)
+    G = args.batches_per_step
     if args.quick:
         if tuned:
             print(json.dumps({"tuned": tuned}), flush=True)
-        elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps, args.warmup, device=True)
+        elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps * G, args.warmup * G,
+                                      device=True)
         if rank == 0:
-            print(json.dumps({"quick": True, "value": args.steps * BATCH / (elapsed_ms * 1e-3),
+            print(json.dumps({"quick": True, "value": args.steps * G * BATCH / (elapsed_ms * 1e-3),
                               "unit": "frames/s", "p99_ms": pct(lat, 99)}), flush=True)
         return
     barrier(world)
     with ClockSampler(local_rank) as clocks:
-        elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps, args.warmup, device=True)
+        elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps * G, args.warmup * G,
+                                      device=True)
     barrier(world)
-    e2e_ms, e2e_lat = run_batched(plans, streams, sets_host, args.steps, args.warmup, device=False)
+    e2e_ms, e2e_lat = run_batched(plans, streams, sets_host, args.steps * G, args.warmup * G,
+                                  device=False)
     barrier(world)
-    elapsed_ms, e2e_ms, value, e2e_value = aggregate_ranks(elapsed_ms, e2e_ms, args.steps, world)
+    elapsed_ms, e2e_ms, value, e2e_value = aggregate_ranks(elapsed_ms, e2e_ms, args.steps, world,
+                                                           batches_per_step=G)
     if rank != 0:
         return
 
@@ -666,12 +710,12 @@ def bench_ours(args, rank, world, local_rank):
 
     for p in plans:
         p.set_stream(None)
-    roof = measure_roofline(plans[0], sets_dev, peaks)
+    roof = measure_roofline(plans[0], sets_dev, peaks, value / world)
     plain = measure_plain(frames, args.plain_frames)
     cpu = measure_cpu_baseline(frames)
     serving = measure_serving(args.serving_seconds, peaks=peaks) if args.serving_seconds > 0 else None
     refine = measure_refine()
-    mixed = measure_mixed_batches(max(200, args.steps // 5), streams=min(args.streams, 8))
+    mixed = measure_mixed_batches(max(200, args.steps * G // 5), streams=min(args.streams, 8))
     result_bytes = BATCH * ((32 + 2 * plans[0].max_detections * 84 + 255) // 256 * 256)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
@@ -679,7 +723,9 @@ def bench_ours(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic",
         "p50_ms": round(pct(lat, 50), 4), "p99_ms": round(pct(lat, 99), 4),
-        "config": {"workload": WORKLOAD, "batch_frames": BATCH, "streams": args.streams,
+        "config": {"workload": WORKLOAD, "batch_frames": BATCH, "batches_per_step": G,
+                   "step": f"{G} batches of {BATCH} frames issued round-robin over {args.streams} "
+                           f"streams", "streams": args.streams,
                    "launch": tuned, "tuning_trials": tune_trials,
                    "frames_pool": POOL, "families_per_frame": 2,
                    "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
@@ -687,7 +733,7 @@ def bench_ours(args, rank, world, local_rank):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e_value, 2), "unit": "frames/s",
                 "p50_ms": round(pct(e2e_lat, 50), 4), "p99_ms": round(pct(e2e_lat, 99), 4),
-                "h2d_bytes_per_step": BATCH * W * H, "d2h_bytes_per_step": result_bytes,
+                "h2d_bytes_per_step": G * BATCH * W * H, "d2h_bytes_per_step": G * result_bytes,
                 "path": "bd_batch_submit_host/bd_batch_wait, frames in pinned host memory"},
         "plain": plain,
         "speedup_vs_plain": round(value / plain["value"], 2),
@@ -700,7 +746,7 @@ def bench_ours(args, rank, world, local_rank):
         "clocks": clocks.summary(),
         # k_stats, k_binarize_runs, k_merge, k_region_stats, k_cand_count,
         # k_fit_decode (+ k_fit_decode_big when the split is on), k_finalize
-        "gpu_launches": (8 if plans[0].launch()["quad_split"] > 0 else 7) * args.steps,
+        "gpu_launches": (8 if plans[0].launch()["quad_split"] > 0 else 7) * args.steps * G,
     }
     print(json.dumps(line), flush=True)
 
@@ -708,8 +754,10 @@ def bench_ours(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10000)
-    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--batches-per-step", type=int, default=32,
+                    help="4-camera batches per step, issued round-robin over the streams")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     # 12 batches in flight: the GPU's saturated rate (12: 128k frames/s, p99
     # 0.45 ms; 8: 117k, 0.32 ms; 16-48 streams: 125-127k at higher p99).

@@ -13,6 +13,9 @@ if [ ! -d "$REF/detector/bench" ]; then
     exit 0
 fi
 mkdir -p "$HERE/_ref"
+# Where the checkout was found, for the tests that read the reference's
+# Python tools (tests/test_reference_consumers.py).
+(cd "$REF" && pwd) > "$HERE/_ref/REFERENCE_DIR"
 g++ -O2 -std=c++20 -I"$REF/detector/src" -I"$REF/detector/tests" \
     "$REF/detector/bench/scene_gen.cpp" -o "$HERE/_ref/bdcudatag_scenes"
 echo "built $HERE/_ref/bdcudatag_scenes"

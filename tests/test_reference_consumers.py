@@ -4,6 +4,7 @@ compile unchanged against include/ and link to libbdcudatag.so with every
 symbol resolved, and its Python ctypes backend
 (detector/bench/compare_detectors.py:71-209) binds this library."""
 import importlib.util
+import os
 import re
 import subprocess
 import sys
@@ -13,9 +14,22 @@ import pytest
 
 import bdcudatag
 
-REF = Path("/root/reference/detector")
 REPO = Path(__file__).resolve().parent.parent
-pytestmark = pytest.mark.skipif(not REF.is_dir(), reason="reference checkout not present")
+
+
+def _reference_dir():
+    """The reference checkout: BD_REFERENCE_DIR, else where oracle/build_ref.sh
+    found it (recorded in oracle/_ref/REFERENCE_DIR), else None."""
+    env = os.environ.get("BD_REFERENCE_DIR")
+    if env:
+        return Path(env)
+    rec = REPO / "oracle" / "_ref" / "REFERENCE_DIR"
+    return Path(rec.read_text().strip()) if rec.exists() else None
+
+
+_ROOT = _reference_dir()
+REF = _ROOT / "detector" if _ROOT else None
+pytestmark = pytest.mark.skipif(REF is None or not REF.is_dir(), reason="reference checkout not present")
 
 
 def test_reference_cpp_consumers_link():
