@@ -10,19 +10,20 @@ namespace bdgb {
 
 // ===========================================================================
 // 1. Tile statistics, histograms, active extents; the last CTA of a frame
-//    computes the frame references and the ROI row count.
+//    computes the frame references and the ROI row count.  A CTA covers
+//    `stats_rows` tile rows; thread i of the CTA takes tile pair i (two
+//    horizontally adjacent tiles, 128-bit loads), row-major over those rows.
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
                                                const FrameIO* __restrict__ io) {
+    constexpr int kMaxStatsRows = 4;
     __shared__ uint32_t s_span[256];
     __shared__ uint32_t s_mean[64];
-    __shared__ int s_lo, s_hi, s_last;
-    __shared__ float s_wb[64], s_sb[64], s_tot[2];
-    __shared__ float s_best_val[2];
-    __shared__ int s_best_idx[2];
+    __shared__ int s_lo[kMaxStatsRows], s_hi[kMaxStatsRows];
+    __shared__ int s_last;
+    __shared__ RefSmem s_ref;
 
     const int tid = threadIdx.x;
-    // CTA c of a frame covers tile rows [c * R, c * R + R), R = stats_rows.
     int fi = 0;
     {
         int lo = 0, hi = b->frames - 1;
@@ -34,84 +35,69 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
     }
     if (!io[fi].gray) return;  // slot not used in this launch
     const FrameDesc& d = b->f[fi];
-    const int R = b->stats_rows;
     const int cta = blockIdx.x - b->stats_prefix[fi];
     const int n_ctas = b->stats_prefix[fi + 1] - b->stats_prefix[fi];
     FrameState* st = d.state;
+    const int ty0 = cta * b->stats_rows;
+    const int nrows = min(b->stats_rows, d.tile_h - ty0);
 
     s_span[tid] = 0;
     if (tid < 64) s_mean[tid] = 0;
+    if (tid < kMaxStatsRows) {
+        s_lo[tid] = INT_MAX;
+        s_hi[tid] = -1;
+    }
+    __syncthreads();
 
     const uint8_t* gray = io[fi].gray;
     const int64_t stride = io[fi].stride;
     const int W = d.width, H = d.height, tw = d.tile_w;
-    const bool vec = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 7u) == 0;
-    const int ty_end = min((cta + 1) * R, d.tile_h);
-    for (int ty = cta * R; ty < ty_end; ++ty) {
-        if (tid == 0) {
-            s_lo = INT_MAX;
-            s_hi = -1;
-        }
-        __syncthreads();
-        const int y0 = ty * kTile;
-        const int rows = min(kTile, H - y0);
-        int lo = INT_MAX, hi = -1;
-        for (int tx = tid; tx < tw; tx += blockDim.x) {
-            const int x0 = tx * kTile;
-            const int cols = min(kTile, W - x0);
-            const uint8_t* p = gray + static_cast<int64_t>(y0) * stride + x0;
-            uint32_t mn, mx, sum = 0;
-            if (vec && cols == kTile) {
-                uint32_t vmin = 0xffffffffu, vmax = 0u;
-                for (int r = 0; r < rows; ++r) {
-                    const uint2 v = *reinterpret_cast<const uint2*>(p + r * stride);
-                    vmin = __vminu4(vmin, __vminu4(v.x, v.y));
-                    vmax = __vmaxu4(vmax, __vmaxu4(v.x, v.y));
-                    sum = __dp4a(v.x, 0x01010101u, sum);
-                    sum = __dp4a(v.y, 0x01010101u, sum);
-                }
-                mn = min(min(vmin & 0xffu, (vmin >> 8) & 0xffu), min((vmin >> 16) & 0xffu, vmin >> 24));
-                mx = max(max(vmax & 0xffu, (vmax >> 8) & 0xffu), max((vmax >> 16) & 0xffu, vmax >> 24));
-            } else {
-                mn = 255u;
-                mx = 0u;
-                for (int r = 0; r < rows; ++r) {
-                    for (int c = 0; c < cols; ++c) {
-                        const uint32_t v = p[r * stride + c];
-                        mn = min(mn, v);
-                        mx = max(mx, v);
-                        sum += v;
-                    }
+    const bool vec16 = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 15u) == 0;
+    const int pairs = (tw + 1) >> 1;
+    const int items = nrows * pairs;
+    // Warp-uniform trip count, so the row groups of a warp reduce together.
+    for (int base = 0; base < items; base += blockDim.x) {
+        const int i = base + tid;
+        int r = 0, lo = INT_MAX, hi = -1;
+        if (i < items) {
+            r = i / pairs;
+            const int pair = i - r * pairs;
+            const int ty = ty0 + r;
+            TileStat t[2];
+            tile_pair_stats(gray, stride, W, H, ty, pair, vec16, &t[0], &t[1]);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (t[k].mn > 255u) continue;  // no second tile in this pair
+                const int tx = 2 * pair + k;
+                const int idx = ty * tw + tx;
+                d.tile_min[idx] = static_cast<uint8_t>(t[k].mn);
+                d.tile_max[idx] = static_cast<uint8_t>(t[k].mx);
+                atomicAdd(&s_span[(t[k].mx - t[k].mn) & 0xffu], 1u);
+                atomicAdd(&s_mean[t[k].mean >> 2], 1u);
+                if (static_cast<int>(t[k].mx - t[k].mn) >= kMinTileContrast) {
+                    lo = min(lo, tx);
+                    hi = max(hi, tx);
                 }
             }
-            const uint32_t count = static_cast<uint32_t>(rows * cols);
-            const uint32_t mean = count == 64u ? (sum + 32u) >> 6 : (sum + count / 2) / count;
-            const int idx = ty * tw + tx;
-            d.tile_min[idx] = static_cast<uint8_t>(mn);
-            d.tile_max[idx] = static_cast<uint8_t>(mx);
-            atomicAdd(&s_span[(mx - mn) & 0xffu], 1u);
-            atomicAdd(&s_mean[mean >> 2], 1u);
-            if (static_cast<int>(mx - mn) >= kMinTileContrast) {
-                lo = min(lo, tx);
-                hi = max(hi, tx);
-            }
         }
-        lo = __reduce_min_sync(kFull, lo);
-        hi = __reduce_max_sync(kFull, hi);
-        if ((tid & 31) == 0 && hi >= 0) {
-            atomicMin(&s_lo, lo);
-            atomicMax(&s_hi, hi);
+        const unsigned peers = __match_any_sync(kFull, r);
+        lo = __reduce_min_sync(peers, lo);
+        hi = __reduce_max_sync(peers, hi);
+        if (hi >= 0 && (tid & 31) == __ffs(peers) - 1) {
+            atomicMin(&s_lo[r], lo);
+            atomicMax(&s_hi[r], hi);
         }
-        __syncthreads();
-        if (tid == 0) {
-            d.row_lo[ty] = s_hi >= 0 ? s_lo : -1;
-            d.row_hi[ty] = s_hi;
-            if (s_hi >= 0) {
-                atomicMax(&st->top_enc, static_cast<uint32_t>(d.tile_h - ty));
-                atomicMax(&st->bottom_enc, static_cast<uint32_t>(ty + 1));
-            }
+    }
+    __syncthreads();
+    if (tid < nrows) {
+        const int ty = ty0 + tid;
+        const int hi = s_hi[tid];
+        d.row_lo[ty] = hi >= 0 ? s_lo[tid] : -1;
+        d.row_hi[ty] = hi;
+        if (hi >= 0) {
+            atomicMax(&st->top_enc, static_cast<uint32_t>(d.tile_h - ty));
+            atomicMax(&st->bottom_enc, static_cast<uint32_t>(ty + 1));
         }
-        __syncthreads();
     }
     if (s_span[tid]) atomicAdd(&st->span_hist[tid], s_span[tid]);
     if (tid < 64 && s_mean[tid]) atomicAdd(&st->mean_hist[tid], s_mean[tid]);
@@ -122,99 +108,9 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
     if (!s_last) return;
     __threadfence();
 
-    // --- frame references (reference k_tile_reference :174-230) ---
-    const int lane = tid & 31;
-    if (tid < 32) {
-        // Lower quartile of the span histogram: first bin whose cumulative
-        // count exceeds total / 4.
-        uint32_t v[8];
-        uint32_t local = 0;
-        for (int k = 0; k < 8; ++k) {
-            v[k] = __ldcg(&st->span_hist[lane * 8 + k]);
-            local += v[k];
-        }
-        uint32_t incl = local;
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t n = __shfl_up_sync(kFull, incl, off);
-            if (lane >= off) incl += n;
-        }
-        const uint32_t total = __shfl_sync(kFull, incl, 31);
-        uint32_t span = 0;
-        if (total > 0) {
-            const uint32_t target = total / 4;
-            uint32_t seen = incl - local;
-            int hit = -1;
-            for (int k = 0; k < 8; ++k) {
-                seen += v[k];
-                if (hit < 0 && seen > target) hit = lane * 8 + k;
-            }
-            const unsigned any = __ballot_sync(kFull, hit >= 0);
-            span = static_cast<uint32_t>(__shfl_sync(kFull, hit, __ffs(any) - 1));
-        }
-        if (lane == 0) st->ref[0] = span;
-    } else if (tid == 32) {
-        // Otsu prefix sums, sequential so every float sum is rounded in the
-        // reference's order.
-        float total = 0.0f, sum = 0.0f;
-        for (int i = 0; i < 64; ++i) {
-            const float m = static_cast<float>(__ldcg(&st->mean_hist[i]));
-            total += m;
-            sum += static_cast<float>(i) * m;
-            s_wb[i] = total;
-            s_sb[i] = sum;
-        }
-        s_tot[0] = total;
-        s_tot[1] = sum;
-    }
-    __syncthreads();
-    if (tid < 64) {
-        // Between-class variance of every split; first maximum wins.
-        const float total = s_tot[0], sum = s_tot[1];
-        const float wb = s_wb[tid];
-        const float wa = total - wb;
-        float between = -2.0f;
-        if (total > 0.0f && wb > 0.0f && wa > 0.0f) {
-            const float sb = s_sb[tid];
-            const float mean_below = sb / wb;
-            const float mean_above = (sum - sb) / wa;
-            const float delta = mean_below - mean_above;
-            between = wb * wa * delta * delta;
-        }
-        int idx = tid;
-        for (int off = 16; off > 0; off >>= 1) {
-            const float ov = __shfl_down_sync(kFull, between, off);
-            const int oi = __shfl_down_sync(kFull, idx, off);
-            if (ov > between || (ov == between && oi < idx)) {
-                between = ov;
-                idx = oi;
-            }
-        }
-        if (lane == 0) {
-            s_best_val[tid >> 5] = between;
-            s_best_idx[tid >> 5] = idx;
-        }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        float best = s_best_val[0];
-        int idx = s_best_idx[0];
-        if (s_best_val[1] > best) {
-            best = s_best_val[1];
-            idx = s_best_idx[1];
-        }
-        const int otsu = best > -1.0f ? idx : 0;
-        st->ref[1] = static_cast<uint32_t>(otsu * 4 + 2);
-        // ROI tile rows: every row between the first and last contrasting
-        // tile row, one row of halo each side (reference :314-330, :2117).
-        const uint32_t te = __ldcg(&st->top_enc), be = __ldcg(&st->bottom_enc);
-        uint32_t roi = 0;
-        if (be > 0) {
-            const int top = d.tile_h - static_cast<int>(te);
-            const int bottom = static_cast<int>(be) - 1;
-            roi = static_cast<uint32_t>(min(bottom + 1, d.tile_h - 1) - max(top - 1, 0) + 1);
-        }
-        st->counts[4] = roi;
-    }
+    // Frame references (reference k_tile_reference :174-230) and ROI rows.
+    frame_references(st->span_hist, st->mean_hist, s_ref, &st->ref[0], &st->ref[1]);
+    if (tid == 0) st->counts[4] = roi_tile_rows(__ldcg(&st->top_enc), __ldcg(&st->bottom_enc), d.tile_h);
 }
 
 // ===========================================================================

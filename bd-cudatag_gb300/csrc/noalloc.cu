@@ -21,10 +21,10 @@
 
 #include <climits>
 #include <cstdint>
-#include <mutex>
 
 #include "bdcudatag/bdcudatag.h"
 #include "bdcudatag/bdcudatag_gb300.h"
+#include "kernels_common.cuh"
 #include "pipeline.cuh"
 
 namespace bdgb {
@@ -47,10 +47,10 @@ static_assert(sizeof(NoAllocScratch) <= kNoAllocScratchBytes, "scratch too small
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr unsigned kFull = 0xffffffffu;
-
-// The per-frame part of k_stats (k_front.cu) with explicit buffers: one CTA
-// per tile row; the last CTA turns the histograms into the frame references.
+// The per-frame part of k_stats (k_front.cu) with explicit buffers, built
+// from the same device routines (tile_pair_stats, frame_references,
+// roi_tile_rows): one CTA per tile row, one thread per tile pair; the last
+// CTA turns the histograms into the frame references.
 __global__ void __launch_bounds__(256) k_tile_stats_noalloc(const uint8_t* __restrict__ gray,
                                                             int W, int H, int64_t stride,
                                                             uint8_t* __restrict__ tile_min,
@@ -60,9 +60,7 @@ __global__ void __launch_bounds__(256) k_tile_stats_noalloc(const uint8_t* __res
     __shared__ uint32_t s_span[256];
     __shared__ uint32_t s_mean[64];
     __shared__ int s_lo, s_hi, s_last;
-    __shared__ float s_wb[64], s_sb[64], s_tot[2];
-    __shared__ float s_best_val[2];
-    __shared__ int s_best_idx[2];
+    __shared__ RefSmem s_ref;
 
     const int tid = threadIdx.x;
     const int ty = blockIdx.x;
@@ -76,36 +74,26 @@ __global__ void __launch_bounds__(256) k_tile_stats_noalloc(const uint8_t* __res
     }
     __syncthreads();
 
-    const int y0 = ty * kTile;
-    const int rows = min(kTile, H - y0);
+    const bool vec16 = ((reinterpret_cast<uintptr_t>(gray) | static_cast<uintptr_t>(stride)) & 15u) == 0;
+    const int pairs = (tw + 1) >> 1;
     int lo = INT_MAX, hi = -1;
-    for (int tx = tid; tx < tw; tx += blockDim.x) {
-        const int x0 = tx * kTile;
-        const int cols = min(kTile, W - x0);
-        const uint8_t* p = gray + static_cast<int64_t>(y0) * stride + x0;
-        uint32_t mn = 255u, mx = 0u, sum = 0u;
-        for (int r = 0; r < rows; ++r) {
-            for (int c = 0; c < cols; ++c) {
-                const uint32_t v = p[r * stride + c];
-                mn = min(mn, v);
-                mx = max(mx, v);
-                sum += v;
+    for (int pair = tid; pair < pairs; pair += blockDim.x) {
+        TileStat t[2];
+        tile_pair_stats(gray, stride, W, H, ty, pair, vec16, &t[0], &t[1]);
+        for (int k = 0; k < 2; ++k) {
+            if (t[k].mn > 255u) continue;  // no second tile in this pair
+            const int tx = 2 * pair + k;
+            tile_min[ty * tw + tx] = static_cast<uint8_t>(t[k].mn);
+            tile_max[ty * tw + tx] = static_cast<uint8_t>(t[k].mx);
+            atomicAdd(&s_span[(t[k].mx - t[k].mn) & 0xffu], 1u);
+            atomicAdd(&s_mean[t[k].mean >> 2], 1u);
+            if (static_cast<int>(t[k].mx - t[k].mn) >= kMinTileContrast) {
+                lo = min(lo, tx);
+                hi = max(hi, tx);
             }
         }
-        const uint32_t count = static_cast<uint32_t>(rows * cols);
-        const uint32_t mean = (sum + count / 2) / count;
-        tile_min[ty * tw + tx] = static_cast<uint8_t>(mn);
-        tile_max[ty * tw + tx] = static_cast<uint8_t>(mx);
-        atomicAdd(&s_span[(mx - mn) & 0xffu], 1u);
-        atomicAdd(&s_mean[mean >> 2], 1u);
-        if (static_cast<int>(mx - mn) >= kMinTileContrast) {
-            lo = min(lo, tx);
-            hi = max(hi, tx);
-        }
     }
-    lo = __reduce_min_sync(kFull, lo);
-    hi = __reduce_max_sync(kFull, hi);
-    if ((tid & 31) == 0 && hi >= 0) {
+    if (hi >= 0) {
         atomicMin(&s_lo, lo);
         atomicMax(&s_hi, hi);
     }
@@ -123,117 +111,22 @@ __global__ void __launch_bounds__(256) k_tile_stats_noalloc(const uint8_t* __res
     if (!s_last) return;
     __threadfence();
 
-    const int lane = tid & 31;
-    if (tid < 32) {
-        uint32_t v[8];
-        uint32_t local = 0;
-        for (int k = 0; k < 8; ++k) {
-            v[k] = __ldcg(&sc->span_hist[lane * 8 + k]);
-            local += v[k];
-        }
-        uint32_t incl = local;
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t n = __shfl_up_sync(kFull, incl, off);
-            if (lane >= off) incl += n;
-        }
-        const uint32_t total = __shfl_sync(kFull, incl, 31);
-        uint32_t span = 0;
-        if (total > 0) {
-            const uint32_t target = total / 4;
-            uint32_t seen = incl - local;
-            int hit = -1;
-            for (int k = 0; k < 8; ++k) {
-                seen += v[k];
-                if (hit < 0 && seen > target) hit = lane * 8 + k;
-            }
-            const unsigned any = __ballot_sync(kFull, hit >= 0);
-            span = static_cast<uint32_t>(__shfl_sync(kFull, hit, __ffs(any) - 1));
-        }
-        if (lane == 0) frame_out[0] = span;
-    } else if (tid == 32) {
-        float total = 0.0f, sum = 0.0f;
-        for (int i = 0; i < 64; ++i) {
-            const float m = static_cast<float>(__ldcg(&sc->mean_hist[i]));
-            total += m;
-            sum += static_cast<float>(i) * m;
-            s_wb[i] = total;
-            s_sb[i] = sum;
-        }
-        s_tot[0] = total;
-        s_tot[1] = sum;
-    }
-    __syncthreads();
-    if (tid < 64) {
-        const float total = s_tot[0], sum = s_tot[1];
-        const float wb = s_wb[tid];
-        const float wa = total - wb;
-        float between = -2.0f;
-        if (total > 0.0f && wb > 0.0f && wa > 0.0f) {
-            const float sb = s_sb[tid];
-            const float mean_below = sb / wb;
-            const float mean_above = (sum - sb) / wa;
-            const float delta = mean_below - mean_above;
-            between = wb * wa * delta * delta;
-        }
-        int idx = tid;
-        for (int off = 16; off > 0; off >>= 1) {
-            const float ov = __shfl_down_sync(kFull, between, off);
-            const int oi = __shfl_down_sync(kFull, idx, off);
-            if (ov > between || (ov == between && oi < idx)) {
-                between = ov;
-                idx = oi;
-            }
-        }
-        if (lane == 0) {
-            s_best_val[tid >> 5] = between;
-            s_best_idx[tid >> 5] = idx;
-        }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        float best = s_best_val[0];
-        int idx = s_best_idx[0];
-        if (s_best_val[1] > best) {
-            best = s_best_val[1];
-            idx = s_best_idx[1];
-        }
-        frame_out[1] = static_cast<uint32_t>((best > -1.0f ? idx : 0) * 4 + 2);
-        const uint32_t te = __ldcg(&sc->top_enc), be = __ldcg(&sc->bottom_enc);
-        uint32_t roi = 0;
-        if (be > 0) {
-            const int top = th - static_cast<int>(te);
-            const int bottom = static_cast<int>(be) - 1;
-            roi = static_cast<uint32_t>(min(bottom + 1, th - 1) - max(top - 1, 0) + 1);
-        }
-        frame_out[2] = roi;
-    }
+    frame_references(sc->span_hist, sc->mean_hist, s_ref, &frame_out[0], &frame_out[1]);
+    if (tid == 0) frame_out[2] = roi_tile_rows(__ldcg(&sc->top_enc), __ldcg(&sc->bottom_enc), th);
 }
 
-// Device address of g_noalloc_scratch, looked up once per device.
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void* g_scratch_address[kMaxDevices] = {};
-
+// Device address of g_noalloc_scratch on the current device.  Looked up on
+// every call (the lookup allocates nothing), so it stays right after a
+// device reset or under another context.
 int32_t scratch_address(void** out) {
-    int device = -1;
-    cudaError_t st = cudaGetDevice(&device);
-    if (st != cudaSuccess || device < 0 || device >= kMaxDevices) {
-        set_last_error("bd_tile_stats_device_noalloc: no usable current CUDA device");
+    void* ptr = nullptr;
+    const cudaError_t st = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (st != cudaSuccess || !ptr) {
+        set_last_error("bd_tile_stats_device_noalloc: cudaGetSymbolAddress failed for the "
+                       "scratch array");
         return BD_ERROR_CUDA;
     }
-    const std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_address[device]) {
-        void* ptr = nullptr;
-        st = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (st != cudaSuccess || !ptr) {
-            cudaGetLastError();
-            set_last_error("bd_tile_stats_device_noalloc: cudaGetSymbolAddress failed for the "
-                           "scratch array");
-            return BD_ERROR_CUDA;
-        }
-        g_scratch_address[device] = ptr;
-    }
-    *out = g_scratch_address[device];
+    *out = ptr;
     return BD_OK;
 }
 
@@ -262,17 +155,20 @@ extern "C" int32_t bd_tile_stats_device_noalloc(const uint8_t* gray_device, int3
     const int32_t rc = scratch_address(&scratch);
     if (rc != BD_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    // Both calls return their own status, so an error left pending by
+    // earlier, unrelated work is neither reported here nor cleared.
     cudaError_t st = cudaMemsetAsync(scratch, 0, sizeof(NoAllocScratch), s);
     if (st == cudaSuccess) {
         const int tile_h = (height + kTile - 1) / kTile;
-        k_tile_stats_noalloc<<<tile_h, 256, 0, s>>>(gray_device, width, height, stride,
-                                                    tile_min_device, tile_max_device,
-                                                    static_cast<NoAllocScratch*>(scratch),
-                                                    frame_device);
-        st = cudaGetLastError();
+        const uint8_t* g = gray_device;
+        int w = width, h = height;
+        int64_t stride64 = stride;
+        NoAllocScratch* sc = static_cast<NoAllocScratch*>(scratch);
+        void* args[] = {&g, &w, &h, &stride64, &tile_min_device, &tile_max_device, &sc, &frame_device};
+        st = cudaLaunchKernel(reinterpret_cast<const void*>(k_tile_stats_noalloc), dim3(tile_h), dim3(256),
+                              args, 0, s);
     }
     if (st != cudaSuccess) {
-        cudaGetLastError();
         set_last_error(cudaGetErrorString(st));
         return BD_ERROR_CUDA;
     }

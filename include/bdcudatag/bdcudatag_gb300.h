@@ -274,8 +274,10 @@ BD_API int32_t bd_refine_gauss_newton(const bd_refine_args* args, float* corners
  * without waiting.  Frames up to BD_NOALLOC_MAX_WIDTH x BD_NOALLOC_MAX_HEIGHT
  * are accepted; larger ones return BD_ERROR_INVALID_ARGUMENT.
  *
- * The first call on a device looks up the scratch array's device address
- * (cudaGetSymbolAddress); make that first call before capturing a stream.
+ * Every call looks up the scratch array's device address on the current
+ * device (cudaGetSymbolAddress, which allocates nothing), so the address
+ * stays right after a device reset.  The first call on a device may load the
+ * library's GPU code there; make that first call before capturing a stream.
  * Every call shares the one scratch array per device and clears it first:
  * calls whose GPU work overlaps race and must be serialised by the caller.
  */

@@ -11,64 +11,11 @@ import pytest
 import bdcudatag
 import oracle
 import scenes
+from gpu_checks import check_frame, kat_config, okat_config, same_records
 from helpers import kat_multiple_frame, pose_corners, score
 
 pytestmark = pytest.mark.gpu
 W, H = 640, 480
-
-
-def kat_config(**kw):
-    return bdcudatag.default_config(max_detections=32, min_decision_margin=2.0, **kw)
-
-
-def okat_config(**kw):
-    return oracle.default_config(max_detections=32, min_decision_margin=2.0, **kw)
-
-
-def same_records(a, b):
-    assert a.shape == b.shape
-    assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), (a, b)
-
-
-def check_frame(img, family=0, gcfg=None, ocfg=None, stages=True):
-    """GPU single-frame detect equals the oracle at every stage."""
-    h, w = img.shape
-    det = bdcudatag.Detector(family, w, h, gcfg)
-    n, got = det.detect(img)
-    ref = oracle.Frame(img, family, ocfg)
-    wn, want = ref.detections()
-    assert n == wn
-    same_records(got, want)
-    if stages:
-        rc = det.stage("row_count")
-        assert np.array_equal(rc, ref.stage("row_count"))
-        assert np.array_equal(det.stage("bits"), ref.stage("bits"))
-        valid = np.zeros((h, ref.row_cap), bool)
-        valid[np.arange(ref.row_cap)[None, :] < rc[:, None]] = True
-        valid = valid.ravel()
-        assert np.array_equal(det.stage("runs")[valid], ref.stage("runs")[valid])
-        lab = det.stage("label")[valid]
-        assert np.array_equal(lab, ref.stage("label")[valid])
-        roots = np.unique(lab)
-        assert np.array_equal(det.stage("area")[roots], ref.stage("area")[roots])
-        assert np.array_equal(det.stage("bbox").reshape(-1, 4)[roots], ref.stage("bbox").reshape(-1, 4)[roots])
-        nc = ref.candidate_count
-        assert np.array_equal(det.stage("candidates")[:nc], ref.stage("candidates"))
-        hq = det.stage("hull_quads")[:nc * 8]
-        assert np.array_equal(hq.view(np.uint32), ref.stage("hull_quads")[:nc * 8].view(np.uint32))
-        q = det.stage("quads")[family * ref.max_candidates * 8:][:nc * 8]
-        assert np.array_equal(q.view(np.uint32), ref.stage("quads")[:nc * 8].view(np.uint32))
-        dg = det.stage("decodes")[family * ref.max_candidates:][:nc]
-        do = ref.stage("decodes")
-        assert np.array_equal(dg["id"], do["id"])
-        ok = do["id"] >= 0
-        assert np.array_equal(dg[ok].view(np.uint8), do[ok].view(np.uint8))
-    st = det.stats()
-    c = ref.counts()
-    assert st.runs == c[2] and st.quads == c[3] and st.detections == wn
-    assert st.candidates == min(c[0], ref.max_candidates)
-    assert st.roi_rows == min(c[4] * 8, h)
-    return n, got
 
 
 # --- the reference's own known-answer tests (test_detector.cpp) -------------
@@ -151,22 +98,6 @@ def test_thread_safety():
     [t.start() for t in threads]
     [t.join() for t in threads]
     assert not bad and det.stats().frames == 20
-
-
-# --- the reference's benchmark scenes: bit-exact and published accuracy ------
-
-@pytest.mark.parametrize("w,h", [(640, 480), (1280, 720), (1280, 800), (1920, 1080)])
-def test_reference_scenes(w, h):
-    imgs, ids, corners = scenes.ref_scenes(w, h, 8)
-    tags = found = wrong = 0
-    errs = []
-    for i in range(len(imgs)):
-        n, d = check_frame(imgs[i], 0, bdcudatag.default_config(max_detections=32),
-                           oracle.default_config(max_detections=32), stages=(i < 2))
-        t, f, wr, e = score(d, n, ids[i], corners[i])
-        tags, found, wrong, errs = tags + t, found + f, wrong + wr, errs + e
-    assert found == tags and wrong == 0
-    assert np.median(errs) < 0.3
 
 
 # --- workload frames and edge cases -------------------------------------------

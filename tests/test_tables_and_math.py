@@ -74,3 +74,24 @@ def test_detmath_accuracy():
     assert L.bdo_atan2f(0.0, -0.0) == np.float32(np.pi)
     assert L.bdo_atan2f(-0.0, -0.0) == -np.float32(np.pi)
     assert np.signbit(L.bdo_atan2f(-0.0, 0.0))
+
+
+def test_otsu_prefix_exact_below_2_24():
+    """k_stats replaces the reference's sequential FP32 Otsu prefix sums
+    (gpu_detector.cu:200-229) by an integer scan converted to float while the
+    weighted sum sum_i i * hist[i] is below 2^24: every partial sum is then an
+    integer that FP32 holds exactly, so both give the same bits.  Checked on
+    random histograms up to the bound, with the sequential loop in float32."""
+    rng = np.random.default_rng(11)
+    for trial in range(300):
+        tiles = int(rng.integers(1, 266305))
+        hist = rng.multinomial(tiles, rng.dirichlet(np.full(64, 0.3))).astype(np.int64)
+        if int(np.dot(np.arange(64), hist)) >= (1 << 24):
+            continue
+        total = np.float32(0.0)
+        s = np.float32(0.0)
+        for i in range(64):
+            total = np.float32(total + np.float32(hist[i]))
+            s = np.float32(s + np.float32(i) * np.float32(hist[i]))
+            assert total == np.float32(np.sum(hist[:i + 1]))
+            assert s == np.float32(np.dot(np.arange(i + 1), hist[:i + 1]))
