@@ -8,10 +8,12 @@
 
 #include <algorithm>
 #include <chrono>
+#include <iterator>
 #include <cstring>
 #include <mutex>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "bdcudatag/bdcudatag.h"
@@ -643,141 +645,150 @@ int64_t bd_detector_debug_stage(bd_detector* detector, const char* name, void* d
 
 }  // extern "C"
 
-// --- C++ API (reference detector.cpp:229-382) ----------------------------------
+// --- C++ API --------------------------------------------------------------------
+//
+// bdcudatag::Detector (include/bdcudatag/detector.hpp, the reference's public
+// C++ API) over the C ABI above.  The behaviour the API fixes is kept: the
+// exception types and texts callers may match on, the clamp of the output
+// capacity to max_detections, and a lock that serialises calls on one object
+// (reference detector.cpp:229-382).  Here the owned state is one RAII object:
+// the C handle lives and dies with Impl, so the Detector's special members
+// only move or delete that object.
 
 namespace bdcudatag {
 
-struct Detector::Impl {
-    bd_detector* handle = nullptr;
-    int max_detections = 0;
-    std::vector<bd_detection> scratch;
-    // Serialises callers that share the scratch buffer.
-    std::mutex mutex;
-};
-
-Detector::Detector(Family family, int width, int height, const DetectorConfig& config)
-    : family_(family), width_(width), height_(height) {
-    bd_config native;
-    bd_config_init(&native);
-    native.max_hamming = config.max_hamming;
-    native.min_cluster_pixels = config.min_cluster_pixels;
-    native.min_tag_pixels = config.min_tag_pixels;
-    native.max_detections = config.max_detections;
-    native.max_candidates = config.max_candidates;
-    native.refine_edges = config.refine_edges ? 1 : 0;
-    native.use_cuda_graph = config.use_cuda_graph ? 1 : 0;
-    native.min_decision_margin = config.min_decision_margin;
-    native.decode_sharpening = config.decode_sharpening;
-    int32_t status = BD_OK;
-    impl_ = new Impl();
-    impl_->handle = bd_detector_create(static_cast<int32_t>(family), width, height, &native, &status);
-    if (!impl_->handle) {
-        const std::string message = bd_last_error();
-        delete impl_;
-        impl_ = nullptr;
-        throw std::runtime_error(message.empty() ? "failed to create bdcudatag detector" : message);
-    }
-    impl_->max_detections = std::min(std::max(native.max_detections, 1), 256);
-    impl_->scratch.resize(static_cast<size_t>(impl_->max_detections));
-}
-
-Detector::~Detector() {
-    if (!impl_) return;
-    if (impl_->handle) bd_detector_destroy(impl_->handle);
-    delete impl_;
-}
-
-Detector::Detector(Detector&& other) noexcept
-    : impl_(other.impl_), family_(other.family_), width_(other.width_), height_(other.height_) {
-    other.impl_ = nullptr;
-}
-
-Detector& Detector::operator=(Detector&& other) noexcept {
-    if (this == &other) return *this;
-    if (impl_) {
-        if (impl_->handle) bd_detector_destroy(impl_->handle);
-        delete impl_;
-    }
-    impl_ = other.impl_;
-    family_ = other.family_;
-    width_ = other.width_;
-    height_ = other.height_;
-    other.impl_ = nullptr;
-    return *this;
-}
-
 namespace {
 
-void to_detections(const bd_detection* src, int count, Detection* out) {
-    for (int i = 0; i < count; ++i) {
-        Detection& dst = out[i];
-        dst.id = src[i].id;
-        dst.hamming = src[i].hamming;
-        dst.decision_margin = src[i].decision_margin;
-        for (int k = 0; k < 4; ++k) {
-            dst.corners[static_cast<size_t>(k)][0] = src[i].corners[k * 2 + 0];
-            dst.corners[static_cast<size_t>(k)][1] = src[i].corners[k * 2 + 1];
-        }
-        for (int k = 0; k < 9; ++k) dst.homography[static_cast<size_t>(k)] = src[i].homography[k];
-    }
+constexpr const char* kMovedFrom = "detector has been moved from";
+
+bd_config to_native(const DetectorConfig& c) {
+    bd_config n;
+    bd_config_init(&n);
+    n.max_hamming = c.max_hamming;
+    n.min_cluster_pixels = c.min_cluster_pixels;
+    n.min_tag_pixels = c.min_tag_pixels;
+    n.max_detections = c.max_detections;
+    n.max_candidates = c.max_candidates;
+    n.refine_edges = c.refine_edges ? 1 : 0;
+    n.use_cuda_graph = c.use_cuda_graph ? 1 : 0;
+    n.min_decision_margin = c.min_decision_margin;
+    n.decode_sharpening = c.decode_sharpening;
+    return n;
 }
+
+Detection from_native(const bd_detection& r) {
+    Detection d;
+    d.id = r.id;
+    d.hamming = r.hamming;
+    d.decision_margin = r.decision_margin;
+    for (size_t k = 0; k < d.corners.size(); ++k) d.corners[k] = {r.corners[2 * k], r.corners[2 * k + 1]};
+    std::copy(std::begin(r.homography), std::end(r.homography), d.homography.begin());
+    return d;
+}
+
+Stats from_native(const bd_stats& s) {
+    Stats o;
+    o.frames = s.frames;
+    o.last_gpu_ms = s.last_gpu_ms;
+    o.average_gpu_ms = s.average_gpu_ms;
+    o.last_total_ms = s.last_total_ms;
+    o.runs = s.runs;
+    o.candidates = s.candidates;
+    o.detections = s.detections;
+    o.quads = s.quads;
+    o.roi_rows = s.roi_rows;
+    return o;
+}
+
+using DetectFn = int32_t (*)(bd_detector*, const uint8_t*, int32_t, bd_detection*, int32_t);
 
 }  // namespace
 
-int Detector::detect(const uint8_t* gray, int stride, Detection* out, int out_capacity) {
-    if (!impl_) throw std::runtime_error("detector has been moved from");
-    if (out_capacity < 0 || (out_capacity > 0 && !out)) {
-        throw std::invalid_argument("invalid detection output buffer");
+// The C detector plus the record buffer its results land in before they are
+// converted; the lock covers both.
+struct Detector::Impl {
+    bd_detector* handle = nullptr;
+    std::vector<bd_detection> records;
+    mutable std::mutex lock;
+
+    Impl(Family family, int width, int height, const DetectorConfig& config) {
+        const bd_config native = to_native(config);
+        int32_t status = BD_OK;
+        handle = bd_detector_create(static_cast<int32_t>(family), width, height, &native, &status);
+        if (!handle) {
+            const std::string why = bd_last_error();
+            throw std::runtime_error(why.empty() ? "failed to create bdcudatag detector" : why);
+        }
+        records.resize(static_cast<size_t>(std::clamp(native.max_detections, 1, 256)));
     }
-    if (out_capacity > impl_->max_detections) out_capacity = impl_->max_detections;
-    const std::lock_guard<std::mutex> lock(impl_->mutex);
-    const int count = bd_detector_detect_host(impl_->handle, gray, stride, impl_->scratch.data(),
-                                              out_capacity);
-    if (count < 0) throw std::runtime_error(bd_last_error());
-    const int written = std::min(count, out_capacity);
-    to_detections(impl_->scratch.data(), written, out);
-    return written;
+    ~Impl() { bd_detector_destroy(handle); }
+    Impl(const Impl&) = delete;
+    Impl& operator=(const Impl&) = delete;
+
+    int capacity() const { return static_cast<int>(records.size()); }
+
+    // One call of the host or device entry point; converts what was written.
+    int run(DetectFn fn, const uint8_t* image, int stride, Detection* out, int out_capacity) {
+        if (out_capacity < 0 || (out_capacity > 0 && !out)) {
+            throw std::invalid_argument("invalid detection output buffer");
+        }
+        const int cap = std::min(out_capacity, capacity());
+        const std::lock_guard<std::mutex> hold(lock);
+        const int found = fn(handle, image, stride, records.data(), cap);
+        if (found < 0) throw std::runtime_error(bd_last_error());
+        const int written = std::min(found, cap);
+        std::transform(records.begin(), records.begin() + written, out,
+                       [](const bd_detection& r) { return from_native(r); });
+        return written;
+    }
+};
+
+Detector::Detector(Family family, int width, int height, const DetectorConfig& config)
+    : impl_(new Impl(family, width, height, config)), family_(family), width_(width),
+      height_(height) {}
+
+Detector::~Detector() { delete impl_; }
+
+Detector::Detector(Detector&& other) noexcept
+    : impl_(std::exchange(other.impl_, nullptr)), family_(other.family_), width_(other.width_),
+      height_(other.height_) {}
+
+Detector& Detector::operator=(Detector&& other) noexcept {
+    if (this != &other) {
+        delete std::exchange(impl_, std::exchange(other.impl_, nullptr));
+        family_ = other.family_;
+        width_ = other.width_;
+        height_ = other.height_;
+    }
+    return *this;
+}
+
+int Detector::detect(const uint8_t* gray, int stride, Detection* out, int out_capacity) {
+    if (!impl_) throw std::runtime_error(kMovedFrom);
+    return impl_->run(&bd_detector_detect_host, gray, stride, out, out_capacity);
 }
 
 std::vector<Detection> Detector::detect(const uint8_t* gray, int stride) {
-    if (!impl_) throw std::runtime_error("detector has been moved from");
-    std::vector<Detection> result(static_cast<size_t>(impl_->max_detections));
-    const int count = detect(gray, stride, result.data(), impl_->max_detections);
-    result.resize(static_cast<size_t>(count));
-    return result;
+    if (!impl_) throw std::runtime_error(kMovedFrom);
+    std::vector<Detection> all(static_cast<size_t>(impl_->capacity()));
+    all.resize(static_cast<size_t>(impl_->run(&bd_detector_detect_host, gray, stride, all.data(),
+                                              impl_->capacity())));
+    return all;
 }
 
 int Detector::detectDevice(const uint8_t* gray_device, int stride, Detection* out, int out_capacity) {
-    if (!impl_) throw std::runtime_error("detector has been moved from");
-    if (out_capacity < 0 || (out_capacity > 0 && !out)) {
-        throw std::invalid_argument("invalid detection output buffer");
-    }
-    if (out_capacity > impl_->max_detections) out_capacity = impl_->max_detections;
-    const std::lock_guard<std::mutex> lock(impl_->mutex);
-    const int count = bd_detector_detect_device(impl_->handle, gray_device, stride,
-                                                impl_->scratch.data(), out_capacity);
-    if (count < 0) throw std::runtime_error(bd_last_error());
-    const int written = std::min(count, out_capacity);
-    to_detections(impl_->scratch.data(), written, out);
-    return written;
+    if (!impl_) throw std::runtime_error(kMovedFrom);
+    return impl_->run(&bd_detector_detect_device, gray_device, stride, out, out_capacity);
 }
 
 Stats Detector::stats() const {
     if (!impl_) return {};
-    const std::lock_guard<std::mutex> lock(impl_->mutex);
     bd_stats native;
-    bd_detector_get_stats(impl_->handle, &native);
-    Stats out;
-    out.frames = native.frames;
-    out.last_gpu_ms = native.last_gpu_ms;
-    out.average_gpu_ms = native.average_gpu_ms;
-    out.last_total_ms = native.last_total_ms;
-    out.runs = native.runs;
-    out.candidates = native.candidates;
-    out.detections = native.detections;
-    out.quads = native.quads;
-    out.roi_rows = native.roi_rows;
-    return out;
+    {
+        const std::lock_guard<std::mutex> hold(impl_->lock);
+        bd_detector_get_stats(impl_->handle, &native);
+    }
+    return from_native(native);
 }
 
 }  // namespace bdcudatag
