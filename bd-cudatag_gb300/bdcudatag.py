@@ -85,7 +85,9 @@ class RefineArgs(ctypes.Structure):
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("stats_rows", ctypes.c_int32), ("quad_warps", ctypes.c_int32),
                 ("quad_ctas_per_sm", ctypes.c_int32), ("quad_split", ctypes.c_int32),
-                ("band_cap", ctypes.c_int32)]
+                ("band_cap", ctypes.c_int32), ("fit_merged", ctypes.c_int32),
+                ("persistent", ctypes.c_int32),
+                ("persist_ctas", ctypes.c_int32)]
 
 
 class Camera(ctypes.Structure):
@@ -117,6 +119,7 @@ GB300_SYMBOLS = [
     "bd_server_poll", "bd_server_get_stats",
     "bd_tag_template", "bd_refine_forward", "bd_refine_backward", "bd_refine_gauss_newton",
     "bd_batch_get_launch", "bd_batch_set_launch", "bd_batch_autotune", "bd_batch_pipeline",
+    "bd_batch_debug_persist",
 ]
 
 _LIB = None
@@ -191,6 +194,7 @@ def lib() -> ctypes.CDLL:
         L.bd_server_get_stats.argtypes = [_P, ctypes.POINTER(ServerStats)]
         L.bd_batch_get_launch.argtypes = [_P, ctypes.POINTER(LaunchConfig)]
         L.bd_batch_set_launch.argtypes = [_P, ctypes.POINTER(LaunchConfig)]
+        L.bd_batch_debug_persist.argtypes = [_P, ctypes.c_int64, ctypes.c_int32]
         L.bd_batch_set_launch.restype = ctypes.c_int32
         L.bd_batch_autotune.argtypes = [_P, _P, _P, ctypes.c_int32, ctypes.POINTER(LaunchConfig),
                                         ctypes.POINTER(ctypes.c_float)]
@@ -381,6 +385,12 @@ class Batch:
         rc = lib().bd_batch_set_launch(self.handle, ctypes.byref(lc))
         if rc != 0:
             raise RuntimeError(f"set_launch failed ({rc}): {last_error()}")
+
+    def debug_persist(self, timeout_ns: int = 1_000_000_000, stall_frame: int = -1) -> None:
+        """Test hook of the persistent launch (bd_batch_debug_persist)."""
+        rc = lib().bd_batch_debug_persist(self.handle, int(timeout_ns), int(stall_frame))
+        if rc != 0:
+            raise RuntimeError(f"debug_persist failed ({rc}): {last_error()}")
 
     def autotune(self, frames_device, strides=None, iterations: int = 20):
         self._set(frames_device, strides)

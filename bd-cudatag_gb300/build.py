@@ -29,7 +29,11 @@ LIB = PKG / "libbdcudatag.so"
 SCENES_LIB = PKG / "libbdscenes.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CUDA_SOURCES = ["k_front.cu", "k_quad.cu", "k_finalize.cu", "engine.cu", "noalloc.cu", "refine.cu"]
+CUDA_SOURCES = ["k_front.cu", "k_quad.cu", "k_finalize.cu", "k_persistent.cu", "engine.cu", "noalloc.cu",
+                "refine.cu"]
+# The persistent kernel reads buffers that other CTAs of the same launch
+# wrote: its plain global loads go to L2 (no L1 line can be stale).
+EXTRA_FLAGS = {"k_persistent.cu": ["-Xptxas", "-dlcm=cg"]}
 CXX_SOURCES = ["capi.cpp", "server.cpp"]
 
 
@@ -80,7 +84,8 @@ def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
         obj = BUILD / (name + ".o")
         objects.append(obj)
         if force or _stale(obj, [src] + headers):
-            cmd = [nv, ARCH, "-lineinfo", "-fmad=false", "-c", str(src), "-o", str(obj)] + common
+            cmd = [nv, ARCH, "-lineinfo", "-fmad=false", "-c", str(src), "-o", str(obj)] + common + \
+                EXTRA_FLAGS.get(name, [])
             if verbose_ptxas:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)

@@ -548,6 +548,9 @@ int32_t bd_batch_get_launch(const bd_batch* batch, bd_launch_config* out) {
     out->quad_ctas_per_sm = lc.quad_ctas_per_sm;
     out->quad_split = lc.quad_split;
     out->band_cap = lc.band_cap;
+    out->fit_merged = lc.fit_merged;
+    out->persistent = lc.persistent;
+    out->persist_ctas = lc.persist_ctas;
     return BD_OK;
 }
 
@@ -562,6 +565,9 @@ int32_t bd_batch_set_launch(bd_batch* batch, const bd_launch_config* launch) {
     lc.quad_ctas_per_sm = launch->quad_ctas_per_sm;
     lc.quad_split = launch->quad_split;
     lc.band_cap = launch->band_cap;
+    lc.fit_merged = launch->fit_merged;
+    lc.persistent = launch->persistent;
+    lc.persist_ctas = launch->persist_ctas;
     const std::lock_guard<std::mutex> lock(batch->plan->mutex());
     std::string error;
     if (batch->plan->set_launch(lc, &error) != 0) {
@@ -587,6 +593,20 @@ int32_t bd_batch_autotune(bd_batch* batch, const uint8_t* const* frames_device,
     }
     if (best_out) bd_batch_get_launch(batch, best_out);
     if (best_ms_out) *best_ms_out = ms;
+    return BD_OK;
+}
+
+int32_t bd_batch_debug_persist(bd_batch* batch, int64_t timeout_ns, int32_t stall_frame) {
+    if (!batch) {
+        set_error("null batch");
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
+    const std::lock_guard<std::mutex> lock(batch->plan->mutex());
+    std::string error;
+    if (batch->plan->set_persist_params(timeout_ns, stall_frame, &error) != 0) {
+        set_error(error);
+        return BD_ERROR_INVALID_ARGUMENT;
+    }
     return BD_OK;
 }
 

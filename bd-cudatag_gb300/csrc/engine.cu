@@ -80,6 +80,9 @@ struct Plan::Impl {
     std::vector<size_t> frame_offset;
     FrameState* states = nullptr;
     size_t states_bytes = 0;
+    WorkQueue* queue = nullptr;        // right after the states: one memset clears both
+    size_t queue_bytes = 0;
+    PersistParams persist;
     uint8_t* results_dev = nullptr;
     uint8_t* results_pinned = nullptr;
     size_t results_bytes = 0;
@@ -124,10 +127,17 @@ struct Plan::Impl {
             cudaMemcpyAsync(io_caller, io_staging, sizeof(FrameIO) * host_desc.frames,
                             cudaMemcpyHostToDevice, s);
         }
-        cudaMemsetAsync(states, 0, states_bytes, s);
-        const ForkJoin fork{branch, ev_fork, ev_join};
-        enqueue_pipeline(dev_desc, host_desc, mode == 2 ? io_caller : io_fixed, s, launch_cfg, sm_count,
-                         branch ? &fork : nullptr, events);
+        const FrameIO* io = mode == 2 ? io_caller : io_fixed;
+        if (launch_cfg.persistent && !events) {
+            cudaMemsetAsync(states, 0, states_bytes + queue_bytes, s);
+            enqueue_persistent(dev_desc, host_desc, io, queue, s, launch_cfg, sm_count, persist);
+        } else {
+            // Stage events (profile_device) always time the per-stage launches.
+            cudaMemsetAsync(states, 0, states_bytes, s);
+            const ForkJoin fork{branch, ev_fork, ev_join};
+            enqueue_pipeline(dev_desc, host_desc, io, s, launch_cfg, sm_count, branch ? &fork : nullptr,
+                             events);
+        }
         cudaMemcpyAsync(results_pinned, results_dev, results_bytes, cudaMemcpyDeviceToHost, s);
     }
 
@@ -205,7 +215,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     };
     cudaError_t st = cudaGetDevice(&im.device);
     if (st != cudaSuccess) return fail(cuda_error("cudaGetDevice", st));
-    if (prepare_pipeline() != 0) {
+    if (prepare_pipeline() != 0 || prepare_persistent() != 0) {
         cudaGetLastError();
         return fail("cudaFuncSetAttribute failed");
     }
@@ -238,7 +248,15 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     im.frame_bytes = frame_total;
     const size_t frames_at = carve.take(frame_total);
     im.states_bytes = sizeof(FrameState) * nf;
-    const size_t states_at = carve.take(im.states_bytes);
+    uint32_t queue_capacity = 0;
+    for (const PlanFrame& f : frames) {
+        queue_capacity += queue_items_per_frame((f.height + kTile - 1) / kTile,
+                                                auto_max_candidates(f.width, f.height, config.max_candidates));
+    }
+    im.queue_bytes = offsetof(WorkQueue, items) + sizeof(uint32_t) * queue_capacity;
+    static_assert(sizeof(FrameState) % 16 == 0, "the work queue follows the states");
+    hd.queue_capacity = queue_capacity;
+    const size_t states_at = carve.take(im.states_bytes + im.queue_bytes);
     im.result_stride = align_up(result_bytes(md), 256);
     im.results_bytes = im.result_stride * nf;
     const size_t results_at = carve.take(im.results_bytes);
@@ -305,6 +323,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     uint8_t* base = static_cast<uint8_t*>(im.arena);
     im.frames_dev = base + frames_at;
     im.states = reinterpret_cast<FrameState*>(base + states_at);
+    im.queue = reinterpret_cast<WorkQueue*>(base + states_at + im.states_bytes);
     im.results_dev = base + results_at;
     im.dev_desc = reinterpret_cast<BatchDesc*>(base + desc_at);
     im.io_fixed = reinterpret_cast<FrameIO*>(base + io_fixed_at);
@@ -537,7 +556,9 @@ int Plan::set_launch(const LaunchConfig& lc, std::string* error) {
     if (!(lc.stats_rows == 1 || lc.stats_rows == 2 || lc.stats_rows == 4) ||
         !(lc.quad_warps == 2 || lc.quad_warps == 4 || lc.quad_warps == kMaxQuadWarps) ||
         lc.quad_ctas_per_sm < 1 || lc.quad_ctas_per_sm > 32 || lc.quad_split < 0 ||
-        lc.quad_split > 4096 || lc.band_cap < 256 || lc.band_cap > 2048) {
+        lc.quad_split > 4096 || lc.band_cap < 256 || lc.band_cap > 2048 ||
+        !(lc.fit_merged == 0 || lc.fit_merged == 1) || !(lc.persistent == 0 || lc.persistent == 1) ||
+        lc.persist_ctas < 0 || lc.persist_ctas > 65536) {
         if (error) *error = "launch config out of range";
         return -1;
     }
@@ -601,8 +622,26 @@ int Plan::autotune(const uint8_t* const* frames, const int32_t* strides, int ite
     if (try_values(&LaunchConfig::quad_ctas_per_sm, quad_ctas, 4) != 0) return -1;
     if (try_values(&LaunchConfig::quad_split, quad_split, 5) != 0) return -1;
     if (try_values(&LaunchConfig::band_cap, band_cap, 3) != 0) return -1;
+    const int fit_merged[] = {0, 1};
+    if (try_values(&LaunchConfig::fit_merged, fit_merged, 2) != 0) return -1;
+    const int persistent[] = {0, 1};
+    if (try_values(&LaunchConfig::persistent, persistent, 2) != 0) return -1;
     if (set_launch(best, error) != 0) return -1;
     if (best_ms) *best_ms = best_t;
+    return 0;
+}
+
+int Plan::set_persist_params(int64_t timeout_ns, int stall_frame, std::string* error) {
+    Impl& im = *impl_;
+    if (timeout_ns <= 0 || stall_frame < -1 || stall_frame >= frames()) {
+        if (error) *error = "persistent test parameters out of range";
+        return -1;
+    }
+    if (im.pending && wait(error) != 0) return -1;
+    cudaStreamSynchronize(im.stream);
+    im.persist.timeout_ns = static_cast<uint64_t>(timeout_ns);
+    im.persist.stall_frame = stall_frame;
+    if (config_.use_graph) im.capture_all();
     return 0;
 }
 
@@ -653,6 +692,18 @@ int Plan::wait(std::string* error) {
     if (late != cudaSuccess) {
         if (error) *error = cuda_error("CUDA launch", late);
         return -1;
+    }
+    // The persistent launch reports a wait that ran out (or a queue
+    // overflow) in every frame's result header.
+    for (int i = 0; i < frames(); ++i) {
+        const uint32_t status = result(i)->pad;
+        if (status) {
+            if (error) {
+                *error = (status & kQueueTimeout) ? "persistent launch gave up: a work-queue wait timed out"
+                                                  : "persistent launch gave up: work queue overflow";
+            }
+            return -1;
+        }
     }
     return 0;
 }

@@ -74,6 +74,10 @@ public:
     int autotune(const uint8_t* const* frames, const int32_t* strides, int iterations,
                  float* best_ms, std::string* error);
 
+    // Test hook of the persistent launch: the queue-wait limit, and a frame
+    // (-1: none) one of whose items is withheld so that the wait runs out.
+    int set_persist_params(int64_t timeout_ns, int stall_frame, std::string* error);
+
     // Stream for later submits (a cudaStream_t; null: the plan's own).
     void set_stream(void* stream);
 

@@ -1,6 +1,8 @@
 // Stage 7 (de-duplication, sort, records) and the launch sequence of a
 // batch: prepare_pipeline, stage names, enqueue_pipeline.
 
+#include <atomic>
+
 #include "stage_finalize.cuh"
 
 namespace bdgb {
@@ -11,12 +13,24 @@ __global__ void __launch_bounds__(kFinalThreads) k_finalize(const BatchDesc* __r
 }
 
 
+// Resident CTAs per SM of k_fit_decode_all (its grid fills the GPU once).
+std::atomic<int> g_fit_all_ctas_per_sm{1};
+
 int prepare_pipeline() {
     // Shared memory beyond 48 KB per block needs an opt-in, per device.
     if (cudaFuncSetAttribute(k_binarize_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(band_smem_bytes(kMaxBandCap, BD_MAX_WIDTH / 32))) !=
         cudaSuccess) {
         return -1;
+    }
+    if (cudaFuncSetAttribute(k_fit_decode_all, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(fit_all_smem_bytes())) != cudaSuccess) {
+        return -1;
+    }
+    int per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fit_decode_all, 256, fit_all_smem_bytes()) ==
+        cudaSuccess) {
+        g_fit_all_ctas_per_sm.store(std::max(1, per_sm));
     }
     return cudaFuncSetAttribute(k_fit_decode, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(kMaxQuadWarps * quad_smem_per_warp())) == cudaSuccess
@@ -66,7 +80,13 @@ void enqueue_pipeline(const BatchDesc* dd, const BatchDesc& hd, const FrameIO* i
     for (int f = 0; f < hd.frames; ++f) cands += hd.f[f].max_candidates;
     const int big_grid = std::max(1, std::min(cands, sm_count));
     const size_t quad_smem = warps * quad_smem_per_warp();
-    if (split > 0 && fork && !stage_events) {
+    if (lc.fit_merged) {
+        // One launch for both paths: the big candidates' CTA time is part of
+        // the fit_decode stage, and the fit_decode_big stage stays empty.
+        mark(6);
+        k_fit_decode_all<<<sm_count * g_fit_all_ctas_per_sm.load(), 256, fit_all_smem_bytes(), s>>>(dd, io);
+        mark(7);
+    } else if (split > 0 && fork && !stage_events) {
         // Big candidates on a parallel branch (a fork/join in the graph).
         cudaStream_t s2 = static_cast<cudaStream_t>(fork->stream);
         cudaEventRecord(static_cast<cudaEvent_t>(fork->fork_event), s);

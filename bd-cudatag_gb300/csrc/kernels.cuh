@@ -50,9 +50,12 @@ __global__ void k_region_stats(const BatchDesc* b, const FrameIO* io);
 __global__ void k_cand_count(const BatchDesc* b, const FrameIO* io, int split_px);
 __global__ void k_fit_decode(const BatchDesc* b, const FrameIO* io);
 __global__ void k_fit_decode_big(const BatchDesc* b, const FrameIO* io, int split_px);
+__global__ void k_fit_decode_all(const BatchDesc* b, const FrameIO* io);
 __global__ void k_finalize(const BatchDesc* b);
 
-// Dynamic shared memory of one k_fit_decode warp.
+// Dynamic shared memory of one k_fit_decode warp, and of a k_fit_decode_all
+// CTA (256 threads).
 size_t quad_smem_per_warp();
+size_t fit_all_smem_bytes();
 
 }  // namespace bdgb

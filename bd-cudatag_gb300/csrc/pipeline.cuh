@@ -38,7 +38,7 @@ struct FrameState {
     uint32_t top_enc;        // tile_h - first active tile row (0: none)
     uint32_t bottom_enc;     // last active tile row + 1 (0: none)
     uint32_t ref[2];         // noise-floor span quartile, Otsu level
-    uint32_t done_stats;     // CTAs of the stats stage finished
+    uint32_t done_stats;     // stats units finished (the persistent launch)
     uint32_t done_cands;     // CTAs of the candidate-count stage finished
     uint32_t n_candidates;   // min(counts[0], max_candidates)
     uint32_t n_big;          // candidates above the big-candidate split (front of FrameDesc::fit_list)
@@ -46,7 +46,41 @@ struct FrameState {
     uint32_t span_hist[256];
     uint32_t mean_hist[64];
     uint32_t bin_base[64];   // first flattened position of each area bin
+    // Units finished per stage, for the persistent launch (k_persistent.cu);
+    // the per-stage launches use done_stats and done_cands only.
+    uint32_t done_bin, done_merge, done_region, done_fit, done_final;
+    uint32_t fit_units;      // fit units queued for this frame
+    uint32_t small_next;     // next (small candidate, family) pair a warp takes
+    // Frame 0 only: the next big candidate / small pair of the whole batch
+    // that k_fit_decode_all hands out.
+    uint32_t batch_big_next, batch_small_next;
+    uint32_t pad_state[1];   // size a multiple of 16 bytes (the work queue follows the states)
 };
+
+// Work queue of one batch for the persistent launch: queue positions
+// [0, seed) are the frames' tile-statistics units, implied by the batch
+// descriptor; position seed + s is items[s], published by the CTA that
+// finished the previous stage of a frame.  Zeroed with the frame states
+// before every batch (0 = not yet published).
+struct WorkQueue {
+    uint32_t head;          // next position to claim
+    uint32_t reserve;       // item slots reserved by pushes
+    uint32_t frames_done;   // frames whose last finalize unit ended
+    uint32_t finished;      // 1: every frame is done, or the launch gave up
+    uint32_t status;        // 0, or kQueueTimeout / kQueueOverflow bits
+    uint32_t pad[3];
+    uint32_t items[1];      // `capacity` slots (the array runs on)
+};
+constexpr uint32_t kQueueTimeout = 1u;   // a wait for a queue slot ran out of time
+constexpr uint32_t kQueueOverflow = 2u;  // more items than the queue holds (a bug)
+
+// Item slots a frame can need (everything but its statistics units): four
+// band stages, one fit unit per big candidate or eight (candidate, family)
+// pairs, two finalize units.
+BDGB_HD inline uint32_t queue_items_per_frame(int tile_h, int max_candidates) {
+    return 4u * static_cast<uint32_t>(tile_h) + static_cast<uint32_t>(max_candidates) +
+           static_cast<uint32_t>((2 * max_candidates + 7) / 8) + 2u;
+}
 
 // One decoded candidate (per family): id -1 when nothing decoded.
 struct DecodeOut {
@@ -89,7 +123,8 @@ struct FrameDesc {
     uint32_t* parent;              // slots: union-find, then the root of every run
     uint32_t* area;                // slots (valid at roots)
     uint32_t* bbox;                // 4 * slots (valid at roots)
-    uint32_t* cand_meta;           // slots: bin << 24 | big << 23 | rank in band, or kNone
+    uint32_t* cand_meta;           // slots: per band (at its first slot) bin << 24 | big << 23 |
+                                   // rank in band of each candidate listed in lroots
     uint32_t* lroots;              // slots: per band (at its first slot) the band-local roots
     uint32_t* lroot_count;         // tile_h: band-local roots per band
     uint32_t* band_mode;           // tile_h: bit 0 fallback (one root per run), else bit r: row r
@@ -109,6 +144,7 @@ struct FrameDesc {
 
 struct BatchDesc {
     int32_t frames;
+    uint32_t queue_capacity;              // item slots of the batch's WorkQueue
     int32_t total_bands;
     int32_t band_prefix[kMaxFrames + 1];  // exclusive prefix of tile_h over frames
     int32_t stats_rows;                   // tile rows per k_stats CTA
@@ -125,6 +161,9 @@ struct LaunchConfig {
     int quad_ctas_per_sm = 8;  // persistent fit/decode grid = SMs * this (capped by the work)
     int quad_split = 32;       // candidates with a bbox side above this (px) take a CTA each; 0: none
     int band_cap = 2048;       // runs of a band unioned in shared memory (256..2048); more: fallback
+    int fit_merged = 0;        // 1: big and small candidates in one fit-and-decode launch
+    int persistent = 0;        // 1: the whole batch as one persistent launch (k_persistent.cu)
+    int persist_ctas = 0;      // CTAs of that launch (0: every SM's resident maximum)
 };
 
 // A second stream and two events for the parallel branch of the pipeline
@@ -162,6 +201,13 @@ BDGB_HD inline size_t result_bytes(int max_detections) {
 // cudaEvent_t, recorded before the first kernel and after every kernel, so
 // consecutive events bracket one stage.
 constexpr int kStageCount = 8;
+// The persistent launch: how long a CTA waits for a queue slot before the
+// launch gives up (the status then says so), and a test hook that withholds
+// one item of frame `stall_frame` (-1: none) so that the wait runs out.
+struct PersistParams {
+    uint64_t timeout_ns = 1000000000ull;
+    int stall_frame = -1;
+};
 // Per-device kernel attributes; call with the device current before the
 // first enqueue.  0 on success.
 int prepare_pipeline();
@@ -169,5 +215,12 @@ extern const char* const kStageNames[kStageCount];
 void enqueue_pipeline(const BatchDesc* device_desc, const BatchDesc& host_desc,
                       const FrameIO* device_io, void* stream, const LaunchConfig& launch,
                       int sm_count, const ForkJoin* fork, void* const* stage_events = nullptr);
+
+// The persistent launch of a batch (k_persistent.cu): one kernel whose CTAs
+// pull (frame, stage, unit) items from `queue` until every frame is done.
+int prepare_persistent();
+void enqueue_persistent(const BatchDesc* device_desc, const BatchDesc& host_desc,
+                        const FrameIO* device_io, WorkQueue* queue, void* stream,
+                        const LaunchConfig& launch, int sm_count, const PersistParams& persist);
 
 }  // namespace bdgb

@@ -21,13 +21,13 @@ struct StatsSmem {
     uint32_t span[256];
     uint32_t mean[64];
     int lo[kMaxStatsRowsPerCta], hi[kMaxStatsRowsPerCta];
-    int last;
-    RefSmem ref;
 };
 
 // Static part of stage_binarize's shared memory; the run arrays and bit rows
 // (band_smem_bytes) are a separate dynamic region.
 struct BinSmem {
+    RefSmem ref;
+    uint32_t refs[2];          // the frame references (span quartile, Otsu level)
     uint8_t thresh[BD_MAX_WIDTH / kTile];
     uint8_t vmin[BD_MAX_WIDTH / kTile];
     uint8_t vmax[BD_MAX_WIDTH / kTile];
@@ -52,13 +52,14 @@ struct CandSmem {
 };
 
 // ===========================================================================
-// 1. Tile statistics, histograms, active extents; the last CTA of a frame
-//    computes the frame references and the ROI row count (and returns
-//    true).  CTA `cta` of frame fi covers
+// 1. Tile statistics, histograms and active extents.  The frame references
+//    that the histograms give are computed where they are used, by every
+//    band of stage 2 (the reference's k_tile_reference :174-230 is a single
+//    thread between the two).  CTA `cta` of frame fi covers
 //    `stats_rows` tile rows; thread i of the CTA takes tile pair i (two
 //    horizontally adjacent tiles, 128-bit loads), row-major over those rows.
 // ===========================================================================
-__device__ __forceinline__ bool stage_stats(const BatchDesc* __restrict__ b, const FrameIO* __restrict__ io, int fi,
+__device__ __forceinline__ void stage_stats(const BatchDesc* __restrict__ b, const FrameIO* __restrict__ io, int fi,
                             int cta, StatsSmem& sm) {
     uint32_t* s_span = sm.span;
     uint32_t* s_mean = sm.mean;
@@ -66,7 +67,6 @@ __device__ __forceinline__ bool stage_stats(const BatchDesc* __restrict__ b, con
     int* s_hi = sm.hi;
     const int tid = threadIdx.x;
     const FrameDesc& d = b->f[fi];
-    const int n_ctas = b->stats_prefix[fi + 1] - b->stats_prefix[fi];
     FrameState* st = d.state;
     const int ty0 = cta * b->stats_rows;
     const int nrows = min(b->stats_rows, d.tile_h - ty0);
@@ -89,11 +89,11 @@ __device__ __forceinline__ bool stage_stats(const BatchDesc* __restrict__ b, con
     for (int base = 0; base < items; base += blockDim.x) {
         const int i = base + tid;
         int r = 0, lo = INT_MAX, hi = -1;
+        TileStat t[2] = {{256u, 0u, 0u}, {256u, 0u, 0u}};
         if (i < items) {
             r = i / pairs;
             const int pair = i - r * pairs;
             const int ty = ty0 + r;
-            TileStat t[2];
             tile_pair_stats(gray, stride, W, H, ty, pair, vec16, &t[0], &t[1]);
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
@@ -102,13 +102,24 @@ __device__ __forceinline__ bool stage_stats(const BatchDesc* __restrict__ b, con
                 const int idx = ty * tw + tx;
                 d.tile_min[idx] = static_cast<uint8_t>(t[k].mn);
                 d.tile_max[idx] = static_cast<uint8_t>(t[k].mx);
-                atomicAdd(&s_span[(t[k].mx - t[k].mn) & 0xffu], 1u);
-                atomicAdd(&s_mean[t[k].mean >> 2], 1u);
                 if (static_cast<int>(t[k].mx - t[k].mn) >= kMinTileContrast) {
                     lo = min(lo, tx);
                     hi = max(hi, tx);
                 }
             }
+        }
+        // Histogram counts, one shared-memory atomic per distinct bin of the
+        // warp: flat regions give most tiles of a row the same span and mean.
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const bool valid = i < items && t[k].mn <= 255u;
+            const uint32_t span_bin = valid ? ((t[k].mx - t[k].mn) & 0xffu) : kNone;
+            const uint32_t mean_bin = valid ? (t[k].mean >> 2) : kNone;
+            const unsigned sp = __match_any_sync(kFull, span_bin);
+            const unsigned mp = __match_any_sync(kFull, mean_bin);
+            const int me = tid & 31;
+            if (valid && me == __ffs(sp) - 1) atomicAdd(&s_span[span_bin], static_cast<uint32_t>(__popc(sp)));
+            if (valid && me == __ffs(mp) - 1) atomicAdd(&s_mean[mean_bin], static_cast<uint32_t>(__popc(mp)));
         }
         const unsigned peers = __match_any_sync(kFull, r);
         lo = __reduce_min_sync(peers, lo);
@@ -131,17 +142,6 @@ __device__ __forceinline__ bool stage_stats(const BatchDesc* __restrict__ b, con
     }
     if (s_span[tid]) atomicAdd(&st->span_hist[tid], s_span[tid]);
     if (tid < 64 && s_mean[tid]) atomicAdd(&st->mean_hist[tid], s_mean[tid]);
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) sm.last = atomicAdd(&st->done_stats, 1u) == static_cast<uint32_t>(n_ctas - 1);
-    __syncthreads();
-    if (!sm.last) return false;
-    __threadfence();
-
-    // Frame references (reference k_tile_reference :174-230) and ROI rows.
-    frame_references(st->span_hist, st->mean_hist, sm.ref, &st->ref[0], &st->ref[1]);
-    if (tid == 0) st->counts[4] = roi_tile_rows(__ldcg(&st->top_enc), __ldcg(&st->bottom_enc), d.tile_h);
-    return true;
 }
 
 // ===========================================================================
@@ -193,6 +193,18 @@ __device__ __forceinline__ void stage_binarize(const BatchDesc* __restrict__ b, 
     const int top = th - static_cast<int>(st->top_enc);
     const int bottom = static_cast<int>(st->bottom_enc) - 1;
     const bool on = bottom >= 0 && ty >= top - 1 && ty <= bottom + 1;
+    // Frame references from the complete histograms (reference
+    // k_tile_reference :174-230): every band that thresholds computes them,
+    // and band 0 also records them and the ROI row count (:2117).
+    if (on || ty == 0) {
+        frame_references(st->span_hist, st->mean_hist, sm.ref, &sm.refs[0], &sm.refs[1]);
+        __syncthreads();
+        if (ty == 0 && tid == 0) {
+            st->ref[0] = sm.refs[0];
+            st->ref[1] = sm.refs[1];
+            st->counts[4] = roi_tile_rows(st->top_enc, st->bottom_enc, th);
+        }
+    }
     if (!on) {
         for (int i = tid; i < rows * words; i += blockDim.x) {
             d.bits[static_cast<int64_t>(y0 + i / words) * words + i % words] = 0xffffffffu;
@@ -213,7 +225,7 @@ __device__ __forceinline__ void stage_binarize(const BatchDesc* __restrict__ b, 
     const int wx_hi = end >> 2;
 
     // Pooled thresholds (reference k_tile_threshold :237-270).
-    const uint32_t ref0 = st->ref[0], ref1 = st->ref[1];
+    const uint32_t ref0 = sm.refs[0], ref1 = sm.refs[1];
     const int floor_contrast = max(kMinTileContrast, static_cast<int>((ref0 * 3) / 2));
     const int t_end = min(4 * wx_hi + 3, tw - 1);
     // The 3x3 window min/max, separably: columns over the three tile rows
@@ -731,8 +743,10 @@ __device__ __forceinline__ bool stage_cand(const BatchDesc* __restrict__ b, int 
     const uint32_t total = s_rowoff[kTile];
     const int w = tid >> 5, lane = tid & 31;
     // The band's candidate roots are listed in its lroots range (free since
-    // k_region_stats), for the frame's last CTA to place.
+    // k_region_stats), and their bin / rank words at the same positions of
+    // cand_meta, for the frame's last CTA to place.
     uint32_t* band_list = d.lroots + static_cast<int64_t>(ty) * kTile * row_cap;
+    uint32_t* band_meta = d.cand_meta + static_cast<int64_t>(ty) * kTile * row_cap;
     for (uint32_t base = 0; base < total; base += blockDim.x) {
         const uint32_t i = base + tid;
         int bin = -1;
@@ -768,8 +782,9 @@ __device__ __forceinline__ bool stage_cand(const BatchDesc* __restrict__ b, int 
             s_run[tid] += add;
         }
         if (bin >= 0) {
-            d.cand_meta[slot] = meta;
-            band_list[atomicAdd(&sm.ncand, 1u)] = slot;
+            const uint32_t at = atomicAdd(&sm.ncand, 1u);
+            band_list[at] = slot;
+            band_meta[at] = meta;
         }
         __syncthreads();  // s_wbin is cleared for the next chunk
     }
@@ -845,25 +860,47 @@ __device__ __forceinline__ bool stage_cand(const BatchDesc* __restrict__ b, int 
     __syncthreads();
     const uint32_t all = s_cprefix[th];
     const uint32_t limit = sm.limit;
-    for (uint32_t j = tid; j < all; j += blockDim.x) {
-        int lo = 0, hi = th - 1;  // last band with s_cprefix[band] <= j
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_cprefix[mid] <= j) lo = mid; else hi = mid - 1;
+    // Four candidates per thread and pass, their loads in flight together:
+    // slot and bin word (one position of both band lists), then the band's
+    // bin prefix.
+    constexpr int kUnroll = 4;
+    for (uint32_t j0 = tid; j0 < all; j0 += kUnroll * blockDim.x) {
+        uint32_t slot[kUnroll], meta[kUnroll], prev[kUnroll];
+        int band[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const uint32_t j = j0 + u * blockDim.x;
+            band[u] = -1;
+            if (j < all) {
+                int lo = 0, hi = th - 1;  // last band with s_cprefix[band] <= j
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_cprefix[mid] <= j) lo = mid; else hi = mid - 1;
+                }
+                band[u] = lo;
+                const int64_t at = static_cast<int64_t>(lo) * kTile * row_cap + (j - s_cprefix[lo]);
+                slot[u] = __ldcg(&d.lroots[at]);
+                meta[u] = __ldcg(&d.cand_meta[at]);
+            }
         }
-        const uint32_t slot = __ldcg(&d.lroots[static_cast<int64_t>(lo) * kTile * row_cap + (j - s_cprefix[lo])]);
-        const uint32_t meta = __ldcg(&d.cand_meta[slot]);
-        const uint32_t cbin = meta >> 24;
-        const uint32_t pos = s_base[cbin] + __ldcg(&d.band_bins[lo * 64 + cbin]) + (meta & 0x7fffffu);
-        if (pos < limit) {
-            d.candidates[pos] = slot;
-            // The fit/decode work lists, split by size once here: big
-            // candidates (a CTA each) from the front, the others (a warp
-            // per family) from the back.
-            if (meta & (1u << 23)) {
-                d.fit_list[atomicAdd(&sm.nbig, 1u)] = pos;
-            } else {
-                d.fit_list[d.max_candidates - 1 - static_cast<int>(atomicAdd(&sm.nsmall, 1u))] = pos;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            if (band[u] >= 0) prev[u] = __ldcg(&d.band_bins[band[u] * 64 + (meta[u] >> 24)]);
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            if (band[u] < 0) continue;
+            const uint32_t pos = s_base[meta[u] >> 24] + prev[u] + (meta[u] & 0x7fffffu);
+            if (pos < limit) {
+                d.candidates[pos] = slot[u];
+                // The fit/decode work lists, split by size once here: big
+                // candidates (a CTA each) from the front, the others (a warp
+                // per family) from the back.
+                if (meta[u] & (1u << 23)) {
+                    d.fit_list[atomicAdd(&sm.nbig, 1u)] = pos;
+                } else {
+                    d.fit_list[d.max_candidates - 1 - static_cast<int>(atomicAdd(&sm.nsmall, 1u))] = pos;
+                }
             }
         }
     }

@@ -88,13 +88,25 @@ BD_API int32_t bd_batch_set_stream(bd_batch* batch, void* cuda_stream);
  *                     many pixels are fitted and decoded by a whole CTA on a
  *                     parallel branch instead (0: none; 0..4096)
  *   band_cap          runs of an 8-row band labelled in shared memory
- *                     (256..2048); a band with more takes the global path */
+ *                     (256..2048); a band with more takes the global path
+ *   fit_merged        1: big and small candidates are fitted and decoded by
+ *                     one launch (no parallel branch in the graph); 0: two
+ *                     launches, the big candidates' on a parallel branch
+ *   persistent        0: one launch per stage (a CUDA graph of seven or
+ *                     eight kernels); 1: the whole batch as one persistent
+ *                     kernel whose CTAs pull (frame, stage, unit) items from
+ *                     a device work queue.  Same results either way.
+ *   persist_ctas      CTAs of the persistent launch (0: every SM's resident
+ *                     maximum; 1..65536) */
 typedef struct bd_launch_config {
     int32_t stats_rows;
     int32_t quad_warps;
     int32_t quad_ctas_per_sm;
     int32_t quad_split;
     int32_t band_cap;
+    int32_t fit_merged;
+    int32_t persistent;
+    int32_t persist_ctas;
 } bd_launch_config;
 
 BD_API int32_t bd_batch_get_launch(const bd_batch* batch, bd_launch_config* out);
@@ -107,6 +119,14 @@ BD_API int32_t bd_batch_set_launch(bd_batch* batch, const bd_launch_config* laun
 BD_API int32_t bd_batch_autotune(bd_batch* batch, const uint8_t* const* frames_device,
                                  const int32_t* strides, int32_t iterations,
                                  bd_launch_config* best_out, float* best_ms_out);
+
+/* Test hook of the persistent launch: sets how long a CTA waits for a work
+ * queue item before the launch gives up (timeout_ns > 0; default one second)
+ * and, with stall_frame >= 0, withholds one work item of that frame, so that
+ * a wait runs out: the batch then ends with BD_ERROR_CUDA and
+ * "persistent launch gave up: a work-queue wait timed out", and the CUDA
+ * context stays usable.  stall_frame -1 restores normal operation. */
+BD_API int32_t bd_batch_debug_persist(bd_batch* batch, int64_t timeout_ns, int32_t stall_frame);
 
 /* Pipeline stages, in launch order (for bd_batch_profile_device). */
 BD_API int32_t bd_stage_count(void);
@@ -296,7 +316,7 @@ BD_API int32_t bd_tile_stats_device_noalloc(const uint8_t* gray_device, int32_t 
 static_assert(sizeof(bd_camera) == 16, "bd_camera layout changed");
 static_assert(sizeof(bd_server_stats) == 56, "bd_server_stats layout changed");
 static_assert(sizeof(bd_refine_args) == 72, "bd_refine_args layout changed");
-static_assert(sizeof(bd_launch_config) == 20, "bd_launch_config layout changed");
+static_assert(sizeof(bd_launch_config) == 32, "bd_launch_config layout changed");
 #endif
 
 #endif /* BDCUDATAG_BDCUDATAG_GB300_H */

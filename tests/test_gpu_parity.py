@@ -227,7 +227,9 @@ def test_launch_shapes_and_autotune_keep_results():
     found, out = batch.detect(dev, strides, device=True)
     shapes = [dict(stats_rows=2, band_cap=256), dict(stats_rows=4, quad_warps=2, quad_split=0),
               dict(quad_ctas_per_sm=1, quad_warps=2, quad_split=16, band_cap=512),
-              dict(stats_rows=1, quad_warps=8, quad_ctas_per_sm=16, quad_split=96, band_cap=2048)]
+              dict(stats_rows=1, quad_warps=8, quad_ctas_per_sm=16, quad_split=96, band_cap=2048),
+              dict(fit_merged=1), dict(fit_merged=1, quad_split=0),
+              dict(fit_merged=1, quad_split=16, band_cap=512)]
     for shape in shapes:
         batch.set_launch(**shape)
         f2, o2 = batch.detect(dev, strides, device=True)
@@ -297,8 +299,9 @@ def test_gpu_corners_against_fp64_refit():
     assert np.nanmedian(rel[same]) < 1e-4
 
 
+@pytest.mark.parametrize("merged", [0, 1])
 @pytest.mark.parametrize("split", [0, 32, 48, 96])
-def test_fit_work_lists_split_candidates_by_size(split):
+def test_fit_work_lists_split_candidates_by_size(split, merged):
     """k_cand_count's placing CTA lists the candidates above the split (for
     the CTA path) and the rest (for the warp path); every candidate is on
     exactly one list, and the results do not depend on the split."""
@@ -308,7 +311,7 @@ def test_fit_work_lists_split_candidates_by_size(split):
               scenes.render_scene(scenes.EIGHT_TAGS_640, 3, 640, 480)[0],
               scenes.render_scene(scenes.MULTI_SIZE, 9, 1920, 1080)[0]]
     batch = bdcudatag.Batch([(w, h, 3) for w, h in sizes])
-    batch.set_launch(quad_split=split)
+    batch.set_launch(quad_split=split, fit_merged=merged)
     found, out = batch.detect([torch.from_numpy(f).cuda() for f in frames], [w for w, _ in sizes],
                               device=True)
     for i, img in enumerate(frames):

@@ -81,3 +81,48 @@ def test_admission_and_rejection():
     rc, found, out, _ = server.wait(t3)
     assert found[0] == n and out[0, :n].tobytes() == d.tobytes()
     server.close()
+
+
+def test_pressure_batches_and_refuses():
+    """Submissions outpace completions: one batch plan in flight (a 3840x2160
+    camera makes each launch long), every camera bursts six frames into a
+    queue two deep.  The queue refuses the rest (admission), the waiting
+    frames of several cameras share launches (continuous batching), and each
+    admitted frame's result still equals detecting it alone."""
+    torch = pytest.importorskip("torch")
+    cams = [(3840, 2160, 3), (1280, 800, 3), (1280, 800, 1), (640, 480, 2)]
+    burst, depth = 6, 2
+    frames = {}
+    for c, (w, h, _) in enumerate(cams):
+        imgs, _ = scenes.render_many(scenes.SERVING, [(w, h)] * burst,
+                                     base=scenes.base_seed(scenes.SERVING) + 700 + 50 * c)
+        pinned = torch.empty((burst, h, w), dtype=torch.uint8, pin_memory=True)
+        pinned.numpy()[:] = np.stack(imgs)
+        frames[c] = (imgs, pinned)
+    server = bdcudatag.Server(cams, max_batches=1, queue_depth=depth)
+    accepted, refused = [], 0
+    for k in range(burst):
+        for c in range(len(cams)):
+            t = server.submit(c, frames[c][1][k])
+            if t >= 0:
+                accepted.append((c, k, t))
+            else:
+                assert t == bdcudatag.ERROR_OUT_OF_MEMORY
+                refused += 1
+    assert refused == (burst - depth) * len(cams)
+    results = {(c, k): server.wait(t) for c, k, t in accepted}
+    st = server.stats()
+    assert st.rejected == refused and st.completed == len(accepted) == depth * len(cams)
+    assert st.mean_batch_frames > 1.0, st.mean_batch_frames
+    for (c, k), (rc, found, out, _) in results.items():
+        assert rc == 1
+        w, h, fams = cams[c]
+        ref = alone(frames[c][0][k], w, h, fams)
+        for fam in (0, 1):
+            if fam not in ref:
+                assert found[fam] == -1
+                continue
+            n, d = ref[fam]
+            assert found[fam] == n
+            assert out[fam, :n].tobytes() == d.tobytes()
+    server.close()
