@@ -87,6 +87,7 @@ __device__ __forceinline__ void stage_stats(const BatchDesc* __restrict__ b, con
     const int items = nrows * pairs;
     // Warp-uniform trip count, so the row groups of a warp reduce together.
     for (int base = 0; base < items; base += blockDim.x) {
+        if (base + (tid & ~31) >= items) continue;  // this warp has no pair in this pass
         const int i = base + tid;
         int r = 0, lo = INT_MAX, hi = -1;
         TileStat t[2] = {{256u, 0u, 0u}, {256u, 0u, 0u}};

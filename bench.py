@@ -727,9 +727,18 @@ def bench_ours(args, rank, world, local_rank):
             print(json.dumps({"tuned": tuned}), flush=True)
         elapsed_ms, lat = run_batched(plans, streams, sets_dev, args.steps * G, args.warmup * G,
                                       device=True)
+        # One batch alone: median GPU time (graph replay, CUDA events) of 50.
+        plans[0].set_stream(None)
+        single = []
+        for k in range(60):
+            plans[0].detect(sets_dev[k % len(sets_dev)], [W] * BATCH, device=True)
+            if k >= 10:
+                single.append(plans[0].last_gpu_ms())
         if rank == 0:
             print(json.dumps({"quick": True, "value": args.steps * G * BATCH / (elapsed_ms * 1e-3),
-                              "unit": "frames/s", "p99_ms": pct(lat, 99)}), flush=True)
+                              "unit": "frames/s", "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+                              "streams": args.streams, "launch": plans[0].launch(),
+                              "single_batch_gpu_ms": float(np.median(single))}), flush=True)
         return
     barrier(world)
     with ClockSampler(local_rank) as clocks:
