@@ -748,46 +748,76 @@ __device__ __forceinline__ bool stage_cand(const BatchDesc* __restrict__ b, int 
     // cand_meta, for the frame's last CTA to place.
     uint32_t* band_list = d.lroots + static_cast<int64_t>(ty) * kTile * row_cap;
     uint32_t* band_meta = d.cand_meta + static_cast<int64_t>(ty) * kTile * row_cap;
-    for (uint32_t base = 0; base < total; base += blockDim.x) {
-        const uint32_t i = base + tid;
-        int bin = -1;
-        bool big = false;
-        uint32_t slot = 0;
-        if (i < total) {
-            slot = band_slot(s_rowoff, y0, row_cap, i);
-            // Two hops reach the root: a run's parent is a band root (or a
-            // root above it after k_merge's path halving), and k_region_stats
-            // pointed every band root at its component's root.
-            const uint32_t root = __ldcg(d.parent + __ldcg(d.parent + slot));
-            d.parent[slot] = root;
-            if (root == slot) bin = candidate_bin(d, slot, split_px, &big);
+    // Up to four chunks of 256 runs at a time: their label and root loads are
+    // issued together, then the chunks are ranked one after another in slot
+    // order, as before.
+    constexpr int kChunks = 4;
+    for (uint32_t gbase = 0; gbase < total; gbase += kChunks * blockDim.x) {
+        int bins[kChunks];
+        bool bigs[kChunks];
+        uint32_t slots[kChunks], hop[kChunks];
+#pragma unroll
+        for (int u = 0; u < kChunks; ++u) {
+            const uint32_t i = gbase + u * blockDim.x + tid;
+            bins[u] = -1;
+            bigs[u] = false;
+            slots[u] = 0;
+            hop[u] = 0;
+            if (i < total) {
+                slots[u] = band_slot(s_rowoff, y0, row_cap, i);
+                hop[u] = __ldcg(d.parent + slots[u]);
+            }
         }
-        const uint32_t key = bin >= 0 ? static_cast<uint32_t>(bin) : 64u + lane;
-        const uint32_t peers = __match_any_sync(kFull, key);
-        const uint32_t rank = __popc(peers & lanemask_lt());
-        s_wbin[w][lane] = 0;
-        s_wbin[w][lane + 32] = 0;
-        __syncthreads();
-        if (bin >= 0 && rank == 0) s_wbin[w][bin] = __popc(peers);
-        __syncthreads();
-        uint32_t meta = kNone;
-        if (bin >= 0) {
-            uint32_t pos = s_run[bin] + rank;
-            for (int w2 = 0; w2 < w; ++w2) pos += s_wbin[w2][bin];
-            meta = (static_cast<uint32_t>(bin) << 24) | (big ? 1u << 23 : 0u) | pos;
+#pragma unroll
+        for (int u = 0; u < kChunks; ++u) {
+            if (gbase + u * blockDim.x + tid < total) {
+                // Two hops reach the root: a run's parent is a band root (or
+                // a root above it after k_merge's path halving), and
+                // k_region_stats pointed every band root at its component's
+                // root.
+                hop[u] = __ldcg(d.parent + hop[u]);
+            }
         }
-        __syncthreads();
-        if (tid < 64) {
-            uint32_t add = 0;
-            for (int w2 = 0; w2 < 8; ++w2) add += s_wbin[w2][tid];
-            s_run[tid] += add;
+#pragma unroll
+        for (int u = 0; u < kChunks; ++u) {
+            if (gbase + u * blockDim.x + tid < total) {
+                d.parent[slots[u]] = hop[u];
+                if (hop[u] == slots[u]) bins[u] = candidate_bin(d, slots[u], split_px, &bigs[u]);
+            }
         }
-        if (bin >= 0) {
-            const uint32_t at = atomicAdd(&sm.ncand, 1u);
-            band_list[at] = slot;
-            band_meta[at] = meta;
+#pragma unroll
+        for (int u = 0; u < kChunks; ++u) {
+            if (gbase + u * blockDim.x >= total) break;  // uniform over the CTA
+            const int bin = bins[u];
+            const bool big = bigs[u];
+            const uint32_t slot = slots[u];
+            const uint32_t key = bin >= 0 ? static_cast<uint32_t>(bin) : 64u + lane;
+            const uint32_t peers = __match_any_sync(kFull, key);
+            const uint32_t rank = __popc(peers & lanemask_lt());
+            s_wbin[w][lane] = 0;
+            s_wbin[w][lane + 32] = 0;
+            __syncthreads();
+            if (bin >= 0 && rank == 0) s_wbin[w][bin] = __popc(peers);
+            __syncthreads();
+            uint32_t meta = kNone;
+            if (bin >= 0) {
+                uint32_t pos = s_run[bin] + rank;
+                for (int w2 = 0; w2 < w; ++w2) pos += s_wbin[w2][bin];
+                meta = (static_cast<uint32_t>(bin) << 24) | (big ? 1u << 23 : 0u) | pos;
+            }
+            __syncthreads();
+            if (tid < 64) {
+                uint32_t add = 0;
+                for (int w2 = 0; w2 < 8; ++w2) add += s_wbin[w2][tid];
+                s_run[tid] += add;
+            }
+            if (bin >= 0) {
+                const uint32_t at = atomicAdd(&sm.ncand, 1u);
+                band_list[at] = slot;
+                band_meta[at] = meta;
+            }
+            __syncthreads();  // s_wbin is cleared for the next chunk
         }
-        __syncthreads();  // s_wbin is cleared for the next chunk
     }
     __syncthreads();
     if (tid < 64) d.band_bins[ty * 64 + tid] = s_run[tid];
@@ -808,32 +838,55 @@ __device__ __forceinline__ bool stage_cand(const BatchDesc* __restrict__ b, int 
     const int q = tid >> 6;
     const int per = (th + 3) >> 2;
     const int qb0 = min(th, q * per), qb1 = min(th, qb0 + per);
+    // Both passes load eight bands at a time, so a quarter of a frame's
+    // bands costs a few L2 round trips instead of one per band.
+    constexpr int kBatch = 8;
     uint32_t sum = 0;
-#pragma unroll 4
-    for (int band = qb0; band < qb1; ++band) sum += __ldcg(&d.band_bins[band * 64 + bin]);
+    for (int band = qb0; band < qb1; band += kBatch) {
+        uint32_t v[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) v[k] = band + k < qb1 ? __ldcg(&d.band_bins[(band + k) * 64 + bin]) : 0u;
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) sum += v[k];
+    }
     s_chunk[q][bin] = sum;
     __syncthreads();
     uint32_t carry = 0;
     for (int q2 = 0; q2 < q; ++q2) carry += s_chunk[q2][bin];
     if (q == 3) s_total[bin] = carry + sum;
-    for (int band = qb0; band < qb1; ++band) {
-        const uint32_t v = __ldcg(&d.band_bins[band * 64 + bin]);
-        d.band_bins[band * 64 + bin] = carry;
-        carry += v;
+    for (int band = qb0; band < qb1; band += kBatch) {
+        uint32_t v[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) v[k] = band + k < qb1 ? __ldcg(&d.band_bins[(band + k) * 64 + bin]) : 0u;
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) {
+            if (band + k < qb1) {
+                d.band_bins[(band + k) * 64 + bin] = carry;
+                carry += v[k];
+            }
+        }
     }
     __syncthreads();
-    if (tid == 0) {
-        uint32_t pos = 0;
-        for (int bin = 0; bin < 64; ++bin) {
-            s_base[bin] = pos;
-            st->bin_base[bin] = pos;
-            pos += s_total[bin];
+    if (tid < 32) {
+        // Exclusive scan of the 64 bin totals: lane l holds bins 2l, 2l + 1.
+        const uint32_t t0 = s_total[2 * lane], t1 = s_total[2 * lane + 1];
+        uint32_t incl = t0 + t1;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t n = __shfl_up_sync(kFull, incl, off);
+            if (lane >= off) incl += n;
         }
-        st->counts[0] = pos;
-        sm.limit = min(pos, static_cast<uint32_t>(d.max_candidates));
-        st->n_candidates = sm.limit;
-        sm.nbig = 0;
-        sm.nsmall = 0;
+        const uint32_t before = incl - t0 - t1;
+        s_base[2 * lane] = before;
+        s_base[2 * lane + 1] = before + t0;
+        st->bin_base[2 * lane] = before;
+        st->bin_base[2 * lane + 1] = before + t0;
+        if (lane == 31) {
+            st->counts[0] = incl;
+            sm.limit = min(incl, static_cast<uint32_t>(d.max_candidates));
+            st->n_candidates = sm.limit;
+            sm.nbig = 0;
+            sm.nsmall = 0;
+        }
     }
 
     // Placement (reference k_order_candidates :642-654): candidate j of the
