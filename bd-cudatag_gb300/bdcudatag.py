@@ -127,92 +127,100 @@ _P = ctypes.c_void_p
 
 
 def lib() -> ctypes.CDLL:
+    """The detector library (libbdcudatag.so next to this file), bound."""
     global _LIB
     if _LIB is None:
         if not LIB_PATH.exists():
             raise RuntimeError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
-        L = ctypes.CDLL(str(LIB_PATH))
-        L.bd_api_version.restype = ctypes.c_uint32
-        L.bd_version_string.restype = ctypes.c_char_p
-        L.bd_family_name.restype = ctypes.c_char_p
-        L.bd_family_name.argtypes = [ctypes.c_int32]
-        for n in ("bd_family_bits_per_side", "bd_family_min_hamming", "bd_family_default_max_hamming"):
-            getattr(L, n).argtypes = [ctypes.c_int32]
-            getattr(L, n).restype = ctypes.c_int32
-        L.bd_config_init.argtypes = [ctypes.POINTER(Config)]
-        L.bd_detector_create.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
-                                         ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_int32)]
-        L.bd_detector_create.restype = _P
-        L.bd_detector_destroy.argtypes = [_P]
-        for n in ("bd_detector_detect_host", "bd_detector_detect_device"):
-            getattr(L, n).argtypes = [_P, _P, ctypes.c_int32, _P, ctypes.c_int32]
-            getattr(L, n).restype = ctypes.c_int32
-        L.bd_detector_get_stats.argtypes = [_P, ctypes.POINTER(Stats)]
-        L.bd_last_error.restype = ctypes.c_char_p
-        L.bd_batch_create.argtypes = [_P, ctypes.c_int32, ctypes.POINTER(Config),
-                                      ctypes.POINTER(ctypes.c_int32)]
-        L.bd_batch_create.restype = _P
-        L.bd_batch_destroy.argtypes = [_P]
-        L.bd_batch_camera_count.argtypes = [_P]
-        L.bd_batch_max_detections.argtypes = [_P]
-        L.bd_batch_device_bytes.argtypes = [_P]
-        L.bd_batch_device_bytes.restype = ctypes.c_int64
-        for n in ("bd_batch_detect_host", "bd_batch_detect_device"):
-            getattr(L, n).argtypes = [_P, _P, _P, _P, _P]
-            getattr(L, n).restype = ctypes.c_int32
-        for n in ("bd_batch_submit_host", "bd_batch_submit_device"):
-            getattr(L, n).argtypes = [_P, _P, _P]
-            getattr(L, n).restype = ctypes.c_int32
-        L.bd_batch_wait.argtypes = [_P, _P, _P]
-        L.bd_batch_wait.restype = ctypes.c_int32
-        L.bd_batch_host_frame.argtypes = [_P, ctypes.c_int32]
-        L.bd_batch_host_frame.restype = _P
-        L.bd_batch_last_gpu_ms.argtypes = [_P]
-        L.bd_batch_last_gpu_ms.restype = ctypes.c_float
-        L.bd_batch_counts.argtypes = [_P, ctypes.c_int32, _P]
-        L.bd_batch_debug_stage.argtypes = [_P, ctypes.c_int32, ctypes.c_char_p, _P, ctypes.c_int64]
-        L.bd_batch_debug_stage.restype = ctypes.c_int64
-        L.bd_detector_debug_stage.argtypes = [_P, ctypes.c_char_p, _P, ctypes.c_int64]
-        L.bd_detector_debug_stage.restype = ctypes.c_int64
-        L.bd_batch_set_stream.argtypes = [_P, _P]
-        L.bd_stage_name.restype = ctypes.c_char_p
-        L.bd_stage_name.argtypes = [ctypes.c_int32]
-        L.bd_batch_profile_device.argtypes = [_P, _P, _P, _P]
-        L.bd_batch_query.argtypes = [_P]
-        L.bd_tile_stats_device_noalloc.argtypes = [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
-                                                   _P, _P, _P, _P]
-        L.bd_tile_stats_device_noalloc.restype = ctypes.c_int32
-        L.bd_server_create.argtypes = [_P, ctypes.c_int32, ctypes.POINTER(Config), ctypes.c_int64,
-                                       ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
-        L.bd_server_create.restype = _P
-        L.bd_server_destroy.argtypes = [_P]
-        L.bd_server_submit.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int32]
-        L.bd_server_submit.restype = ctypes.c_int64
-        for n in ("bd_server_wait", "bd_server_poll"):
-            getattr(L, n).argtypes = [_P, ctypes.c_int64, _P, _P, ctypes.POINTER(ctypes.c_double)]
-            getattr(L, n).restype = ctypes.c_int32
-        L.bd_server_get_stats.argtypes = [_P, ctypes.POINTER(ServerStats)]
-        L.bd_batch_get_launch.argtypes = [_P, ctypes.POINTER(LaunchConfig)]
-        L.bd_batch_set_launch.argtypes = [_P, ctypes.POINTER(LaunchConfig)]
-        L.bd_batch_debug_persist.argtypes = [_P, ctypes.c_int64, ctypes.c_int32]
-        L.bd_batch_set_launch.restype = ctypes.c_int32
-        L.bd_batch_autotune.argtypes = [_P, _P, _P, ctypes.c_int32, ctypes.POINTER(LaunchConfig),
-                                        ctypes.POINTER(ctypes.c_float)]
-        L.bd_batch_autotune.restype = ctypes.c_int32
-        L.bd_batch_pipeline.argtypes = [_P, ctypes.c_int32, _P, _P, ctypes.c_int32, ctypes.c_int32,
-                                        ctypes.c_int32, _P, ctypes.POINTER(ctypes.c_double)]
-        L.bd_batch_pipeline.restype = ctypes.c_int32
-        L.bd_tag_template.argtypes = [ctypes.c_int32, ctypes.c_int32, _P]
-        L.bd_tag_template.restype = ctypes.c_int32
-        L.bd_refine_forward.argtypes = [ctypes.POINTER(RefineArgs), _P, _P, _P]
-        L.bd_refine_forward.restype = ctypes.c_int32
-        L.bd_refine_backward.argtypes = [ctypes.POINTER(RefineArgs), _P, _P, _P, _P]
-        L.bd_refine_backward.restype = ctypes.c_int32
-        L.bd_refine_gauss_newton.argtypes = [ctypes.POINTER(RefineArgs), _P, ctypes.c_int32, _P, _P]
-        L.bd_refine_gauss_newton.restype = ctypes.c_int32
-        L.bd_batch_query.restype = ctypes.c_int32
-        _LIB = L
+        _LIB = load(LIB_PATH)
     return _LIB
+
+
+def load(path) -> ctypes.CDLL:
+    """Loads and binds a build of the library at `path` (for example the
+    reference-arithmetic variant that build.py makes for a test).  Every load
+    has its own symbols and its own CUDA kernels."""
+    L = ctypes.CDLL(str(path))
+    L.bd_api_version.restype = ctypes.c_uint32
+    L.bd_version_string.restype = ctypes.c_char_p
+    L.bd_family_name.restype = ctypes.c_char_p
+    L.bd_family_name.argtypes = [ctypes.c_int32]
+    for n in ("bd_family_bits_per_side", "bd_family_min_hamming", "bd_family_default_max_hamming"):
+        getattr(L, n).argtypes = [ctypes.c_int32]
+        getattr(L, n).restype = ctypes.c_int32
+    L.bd_config_init.argtypes = [ctypes.POINTER(Config)]
+    L.bd_detector_create.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_int32)]
+    L.bd_detector_create.restype = _P
+    L.bd_detector_destroy.argtypes = [_P]
+    for n in ("bd_detector_detect_host", "bd_detector_detect_device"):
+        getattr(L, n).argtypes = [_P, _P, ctypes.c_int32, _P, ctypes.c_int32]
+        getattr(L, n).restype = ctypes.c_int32
+    L.bd_detector_get_stats.argtypes = [_P, ctypes.POINTER(Stats)]
+    L.bd_last_error.restype = ctypes.c_char_p
+    L.bd_batch_create.argtypes = [_P, ctypes.c_int32, ctypes.POINTER(Config),
+                                  ctypes.POINTER(ctypes.c_int32)]
+    L.bd_batch_create.restype = _P
+    L.bd_batch_destroy.argtypes = [_P]
+    L.bd_batch_camera_count.argtypes = [_P]
+    L.bd_batch_max_detections.argtypes = [_P]
+    L.bd_batch_device_bytes.argtypes = [_P]
+    L.bd_batch_device_bytes.restype = ctypes.c_int64
+    for n in ("bd_batch_detect_host", "bd_batch_detect_device"):
+        getattr(L, n).argtypes = [_P, _P, _P, _P, _P]
+        getattr(L, n).restype = ctypes.c_int32
+    for n in ("bd_batch_submit_host", "bd_batch_submit_device"):
+        getattr(L, n).argtypes = [_P, _P, _P]
+        getattr(L, n).restype = ctypes.c_int32
+    L.bd_batch_wait.argtypes = [_P, _P, _P]
+    L.bd_batch_wait.restype = ctypes.c_int32
+    L.bd_batch_host_frame.argtypes = [_P, ctypes.c_int32]
+    L.bd_batch_host_frame.restype = _P
+    L.bd_batch_last_gpu_ms.argtypes = [_P]
+    L.bd_batch_last_gpu_ms.restype = ctypes.c_float
+    L.bd_batch_counts.argtypes = [_P, ctypes.c_int32, _P]
+    L.bd_batch_debug_stage.argtypes = [_P, ctypes.c_int32, ctypes.c_char_p, _P, ctypes.c_int64]
+    L.bd_batch_debug_stage.restype = ctypes.c_int64
+    L.bd_detector_debug_stage.argtypes = [_P, ctypes.c_char_p, _P, ctypes.c_int64]
+    L.bd_detector_debug_stage.restype = ctypes.c_int64
+    L.bd_batch_set_stream.argtypes = [_P, _P]
+    L.bd_stage_name.restype = ctypes.c_char_p
+    L.bd_stage_name.argtypes = [ctypes.c_int32]
+    L.bd_batch_profile_device.argtypes = [_P, _P, _P, _P]
+    L.bd_batch_query.argtypes = [_P]
+    L.bd_tile_stats_device_noalloc.argtypes = [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                               _P, _P, _P, _P]
+    L.bd_tile_stats_device_noalloc.restype = ctypes.c_int32
+    L.bd_server_create.argtypes = [_P, ctypes.c_int32, ctypes.POINTER(Config), ctypes.c_int64,
+                                   ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+    L.bd_server_create.restype = _P
+    L.bd_server_destroy.argtypes = [_P]
+    L.bd_server_submit.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int32]
+    L.bd_server_submit.restype = ctypes.c_int64
+    for n in ("bd_server_wait", "bd_server_poll"):
+        getattr(L, n).argtypes = [_P, ctypes.c_int64, _P, _P, ctypes.POINTER(ctypes.c_double)]
+        getattr(L, n).restype = ctypes.c_int32
+    L.bd_server_get_stats.argtypes = [_P, ctypes.POINTER(ServerStats)]
+    L.bd_batch_get_launch.argtypes = [_P, ctypes.POINTER(LaunchConfig)]
+    L.bd_batch_set_launch.argtypes = [_P, ctypes.POINTER(LaunchConfig)]
+    L.bd_batch_debug_persist.argtypes = [_P, ctypes.c_int64, ctypes.c_int32]
+    L.bd_batch_set_launch.restype = ctypes.c_int32
+    L.bd_batch_autotune.argtypes = [_P, _P, _P, ctypes.c_int32, ctypes.POINTER(LaunchConfig),
+                                    ctypes.POINTER(ctypes.c_float)]
+    L.bd_batch_autotune.restype = ctypes.c_int32
+    L.bd_batch_pipeline.argtypes = [_P, ctypes.c_int32, _P, _P, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.c_int32, _P, ctypes.POINTER(ctypes.c_double)]
+    L.bd_batch_pipeline.restype = ctypes.c_int32
+    L.bd_tag_template.argtypes = [ctypes.c_int32, ctypes.c_int32, _P]
+    L.bd_tag_template.restype = ctypes.c_int32
+    L.bd_refine_forward.argtypes = [ctypes.POINTER(RefineArgs), _P, _P, _P]
+    L.bd_refine_forward.restype = ctypes.c_int32
+    L.bd_refine_backward.argtypes = [ctypes.POINTER(RefineArgs), _P, _P, _P, _P]
+    L.bd_refine_backward.restype = ctypes.c_int32
+    L.bd_refine_gauss_newton.argtypes = [ctypes.POINTER(RefineArgs), _P, ctypes.c_int32, _P, _P]
+    L.bd_refine_gauss_newton.restype = ctypes.c_int32
+    L.bd_batch_query.restype = ctypes.c_int32
+    return L
 
 
 def default_config(**overrides) -> Config:
@@ -259,11 +267,14 @@ def _stage(fn, *args, name: str) -> np.ndarray:
 class Detector:
     """One family, one frame size: the reference's bd_detector."""
 
-    def __init__(self, family: int, width: int, height: int, config: Config | None = None):
+    def __init__(self, family: int, width: int, height: int, config: Config | None = None,
+                 library: ctypes.CDLL | None = None):
+        """library: a build loaded with load() (default: the library)."""
+        self._L = library if library is not None else lib()
         status = ctypes.c_int32(0)
         cfg = config if config is not None else default_config()
-        self.handle = lib().bd_detector_create(family, width, height, ctypes.byref(cfg),
-                                               ctypes.byref(status))
+        self.handle = self._L.bd_detector_create(family, width, height, ctypes.byref(cfg),
+                                                 ctypes.byref(status))
         if not self.handle:
             raise RuntimeError(f"bd_detector_create failed ({status.value}): {last_error()}")
         self.family, self.width, self.height = family, width, height
@@ -274,14 +285,14 @@ class Detector:
         """Returns (found, detections written)."""
         cap = self.max_detections if capacity is None else capacity
         s = gray.strides[0] if stride is None else stride
-        n = lib().bd_detector_detect_host(self.handle, _ptr(gray), s, self.out.ctypes.data, cap)
+        n = self._L.bd_detector_detect_host(self.handle, _ptr(gray), s, self.out.ctypes.data, cap)
         if n < 0:
             raise RuntimeError(f"detect failed ({n}): {last_error()}")
         return n, self.out[:min(n, cap)].copy()
 
     def detect_device(self, gray_device, stride: int, capacity: int | None = None):
         cap = self.max_detections if capacity is None else capacity
-        n = lib().bd_detector_detect_device(self.handle, _ptr(gray_device), stride,
+        n = self._L.bd_detector_detect_device(self.handle, _ptr(gray_device), stride,
                                             self.out.ctypes.data, cap)
         if n < 0:
             raise RuntimeError(f"detect_device failed ({n}): {last_error()}")
@@ -289,15 +300,15 @@ class Detector:
 
     def stats(self) -> Stats:
         s = Stats()
-        lib().bd_detector_get_stats(self.handle, ctypes.byref(s))
+        self._L.bd_detector_get_stats(self.handle, ctypes.byref(s))
         return s
 
     def stage(self, name: str) -> np.ndarray:
-        return _stage(lib().bd_detector_debug_stage, self.handle, name=name)
+        return _stage(self._L.bd_detector_debug_stage, self.handle, name=name)
 
     def close(self) -> None:
         if getattr(self, "handle", None):
-            lib().bd_detector_destroy(self.handle)
+            self._L.bd_detector_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

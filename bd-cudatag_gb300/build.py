@@ -71,8 +71,23 @@ def build_scenes(force: bool = False) -> Path:
     return SCENES_LIB
 
 
-def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
-    BUILD.mkdir(exist_ok=True)
+# The reference-arithmetic variant: the same sources built the way the
+# reference is (nvcc's default multiply-add contraction, CUDA's libm for
+# sin/cos/atan2/hypot).  A test builds and loads it beside the library to
+# measure how far that rounding moves results; it is not shipped.
+REFARITH_LIB = PKG / "libbdcudatag_refarith.so"
+REFARITH_FLAGS = ["-fmad=true", "-DBDGB_CUDA_LIBM"]
+
+
+def build_library(force: bool = False, verbose_ptxas: bool = False, variant: str | None = None) -> Path:
+    """Builds libbdcudatag.so, or with variant="refarith" the
+    reference-arithmetic variant (own object folder and library file)."""
+    if variant not in (None, "refarith"):
+        raise ValueError(f"unknown build variant {variant!r}")
+    build_dir = BUILD if variant is None else PKG / f"_build_{variant}"
+    lib_path = LIB if variant is None else REFARITH_LIB
+    fmad = ["-fmad=false"] if variant is None else REFARITH_FLAGS
+    build_dir.mkdir(exist_ok=True)
     nv = nvcc()
     common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "-DBDCUDATAG_BUILDING", f"-I{INCLUDE}", f"-I{CSRC}"]
@@ -81,17 +96,17 @@ def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
     headers = _headers()
     for name in CUDA_SOURCES:
         src = CSRC / name
-        obj = BUILD / (name + ".o")
+        obj = build_dir / (name + ".o")
         objects.append(obj)
         if force or _stale(obj, [src] + headers):
-            cmd = [nv, ARCH, "-lineinfo", "-fmad=false", "-c", str(src), "-o", str(obj)] + common + \
+            cmd = [nv, ARCH, "-lineinfo"] + fmad + ["-c", str(src), "-o", str(obj)] + common + \
                 EXTRA_FLAGS.get(name, [])
             if verbose_ptxas:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)
     for name in CXX_SOURCES:
         src = CSRC / name
-        obj = BUILD / (name + ".o")
+        obj = build_dir / (name + ".o")
         objects.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden",
@@ -101,10 +116,10 @@ def build_library(force: bool = False, verbose_ptxas: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as pool:
         for f in [pool.submit(_run, j) for j in jobs]:
             f.result()
-    if force or jobs or _stale(LIB, objects):
-        _run([nv, ARCH, "-shared", "-o", str(LIB)] + [str(o) for o in objects] +
+    if force or jobs or _stale(lib_path, objects):
+        _run([nv, ARCH, "-shared", "-o", str(lib_path)] + [str(o) for o in objects] +
              ["-lcudart", "-lpthread"])
-    return LIB
+    return lib_path
 
 
 def build_all(force: bool = False) -> None:

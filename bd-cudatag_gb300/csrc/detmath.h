@@ -49,6 +49,19 @@ BDM_FN float quiet_nan() {
     return f;
 }
 
+#if defined(BDGB_CUDA_LIBM) && defined(__CUDA_ARCH__)
+// The reference-arithmetic build (build.py, variant "refarith"): the
+// kernels call CUDA's own sinf, cosf, atan2f and hypotf, as the reference's
+// kernels do, and are compiled with multiply-add contraction on.  It exists
+// to measure, on the GPU, how far the reference's rounding moves results
+// from this project's default arithmetic; the oracle does not reproduce it.
+BDM_FN void sincos(float x, float* s_out, float* c_out) {
+    *s_out = ::sinf(x);
+    *c_out = ::cosf(x);
+}
+BDM_FN float atan2(float y, float x) { return ::atan2f(y, x); }
+BDM_FN float hypot(float x, float y) { return ::hypotf(x, y); }
+#else
 // sin and cos of x for |x| < 1000.
 BDM_FN void sincos(float x, float* s_out, float* c_out) {
     const float kTwoOverPi = 0x1.45f306p-1f;
@@ -143,5 +156,6 @@ BDM_FN float atan2(float y, float x) {
 }
 
 BDM_FN float hypot(float x, float y) { return sqrtf(x * x + y * y); }
+#endif
 
 }  // namespace bdmath
