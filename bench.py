@@ -794,9 +794,11 @@ def bench_ours(args, rank, world, local_rank):
         "parity": {"vs_oracle": "bit-exact at every stage (bitmap, runs, labels, area/bbox, "
                                 "candidates, quads, decodes, records); tests/",
                    "vs_reference_build": "not measured: the reference's GPU library cannot run "
-                                         "on the GPU host; a contraction-on CPU build of the "
-                                         "same restatement moves decoded corners by a median "
-                                         "2.4e-3 px and flips 2 of 14,822 candidate decodes"},
+                                         "on the GPU host; built the reference's way (nvcc "
+                                         "contraction, CUDA libm) the same kernels move "
+                                         "decoded corners by a median 3.4e-3 px and flip 2 of "
+                                         "14,005 candidate decodes "
+                                         "(tests/test_gpu_reference_arithmetic.py)"},
         "e2e_speedup_vs_plain": round(e2e_value / plain["value"], 2),
         "roofline": roof,
         "cpu_baseline": cpu,
