@@ -276,11 +276,19 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
     }
 }
 
-__device__ __forceinline__ uint32_t uf_root_readonly(const uint32_t* parent, uint32_t x) {
+// Root of x once every union is done, halving the path as it walks: each
+// node passed is pointed at its grandparent, so walks of the same chain that
+// start later (from other bands) take fewer steps.  The halving link is an
+// atomicMin, so it never raises a link that another walker has already set
+// to the component's root (the smallest slot of the component).
+__device__ __forceinline__ uint32_t uf_root_halving(uint32_t* parent, uint32_t x) {
     for (;;) {
         const uint32_t p = __ldcg(parent + x);
         if (p == x) return x;
-        x = p;
+        const uint32_t gp = __ldcg(parent + p);
+        if (gp == p) return p;
+        atomicMin(parent + x, gp);
+        x = gp;
     }
 }
 

@@ -647,9 +647,9 @@ __device__ __forceinline__ void stage_region(const BatchDesc* __restrict__ b, in
         bool fold = false;
         if (k < n) {
             s = list[k];
-            // All unions are done: walk to the root without compressing
-            // (the band root alone is relinked below).
-            g = uf_root_readonly(d.parent, s);
+            // All unions are done: walk to the root, halving the path for
+            // the other bands' walks (the band root is relinked below).
+            g = uf_root_halving(d.parent, s);
             fold = g != s;
         }
         const unsigned want = __ballot_sync(kFull, fold);
