@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(256) k_stats(const BatchDesc* __restrict__ b,
     stage_stats(b, io, fi, blockIdx.x - b->stats_prefix[fi], sm);
 }
 
-__global__ void __launch_bounds__(256, 4) k_binarize_runs(const BatchDesc* __restrict__ b,
+__global__ void __launch_bounds__(256, 6) k_binarize_runs(const BatchDesc* __restrict__ b,
                                                        const FrameIO* __restrict__ io, int cap,
                                                        int bits_words) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
