@@ -238,7 +238,7 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
     std::vector<size_t> off_frame(nf), off_tmin(nf), off_tmax(nf), off_lo(nf), off_hi(nf),
         off_bits(nf), off_rc(nf), off_runs(nf), off_parent(nf), off_area(nf), off_bbox(nf),
         off_meta(nf), off_bands(nf), off_cands(nf), off_hull(nf), off_quads(nf), off_dec(nf),
-        off_lroots(nf), off_lcount(nf), off_mode(nf), off_dech(nf), off_fit(nf);
+        off_lroots(nf), off_lcount(nf), off_mode(nf), off_fit(nf);
     im.frame_offset.resize(nf);
     size_t frame_total = 0;
     for (int i = 0; i < nf; ++i) {
@@ -308,7 +308,6 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
         off_hull[i] = carve.take(sizeof(float) * 8 * mc);
         off_quads[i] = carve.take(sizeof(float) * 16 * mc);
         off_dec[i] = carve.take(sizeof(DecodeOut) * 2 * mc);
-        off_dech[i] = carve.take(sizeof(float) * 9 * 2 * mc);
     }
     hd.band_prefix[nf] = bands;
     hd.total_bands = bands;
@@ -352,7 +351,6 @@ Plan* Plan::create(const std::vector<PlanFrame>& frames, const PlanConfig& confi
         d.hull_quads = reinterpret_cast<float*>(base + off_hull[i]);
         d.quads = reinterpret_cast<float*>(base + off_quads[i]);
         d.decodes = reinterpret_cast<DecodeOut*>(base + off_dec[i]);
-        d.dec_h = reinterpret_cast<float*>(base + off_dech[i]);
         d.result = reinterpret_cast<FrameResultHeader*>(im.results_dev + im.result_stride * i);
         fixed[i].gray = im.frames_dev + im.frame_offset[i];
         fixed[i].stride = frames[i].width;

@@ -138,7 +138,6 @@ struct FrameDesc {
     float* hull_quads;             // max_candidates * 8
     float* quads;                  // 2 * max_candidates * 8 (per family)
     DecodeOut* decodes;            // 2 * max_candidates
-    float* dec_h;                  // 2 * max_candidates * 9: homography of each decoded candidate
     FrameResultHeader* result;     // header + 2 * max_detections records
 };
 

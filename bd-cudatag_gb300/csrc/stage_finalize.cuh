@@ -12,11 +12,45 @@ namespace {
 struct FinalSmem {
     DecodeOut in[kMaxDetectionsCap];
     DecodeOut out[kMaxDetectionsCap];
-    int in_src[kMaxDetectionsCap], out_src[kMaxDetectionsCap];  // candidate index
     float cx[kMaxDetectionsCap], cy[kMaxDetectionsCap];
     uint32_t warp[kFinalThreads / 32];
     int count, kept;
 };
+
+// Image homography of a final detection's corners (reference host
+// fill_homography :1739-1774, FP64 as there), one detection per thread of
+// the finalizing CTA.
+__device__ void fill_homography(const float corners[8], float H[9]) {
+    const double x0 = corners[0], y0 = corners[1];
+    const double x1 = corners[2], y1 = corners[3];
+    const double x2 = corners[4], y2 = corners[5];
+    const double x3 = corners[6], y3 = corners[7];
+    const double dx1 = x1 - x2, dx2 = x3 - x2;
+    const double dx3 = x0 - x1 + x2 - x3;
+    const double dy1 = y1 - y2, dy2 = y3 - y2;
+    const double dy3 = y0 - y1 + y2 - y3;
+    double g = 0.0, h = 0.0;
+    const double det = dx1 * dy2 - dx2 * dy1;
+    if (fabs(det) > 1e-12) {
+        g = (dx3 * dy2 - dx2 * dy3) / det;
+        h = (dx1 * dy3 - dx3 * dy1) / det;
+    }
+    const double a = x1 - x0 + g * x1;
+    const double bb = x3 - x0 + h * x3;
+    const double dd = y1 - y0 + g * y1;
+    const double e = y3 - y0 + h * y3;
+    const double w = g + h + 2.0;
+    const double inv = (fabs(w) > 1e-12) ? 1.0 / w : 0.0;
+    H[0] = static_cast<float>(a * inv);
+    H[1] = static_cast<float>(bb * inv);
+    H[2] = static_cast<float>((a + bb + 2.0 * x0) * inv);
+    H[3] = static_cast<float>(dd * inv);
+    H[4] = static_cast<float>(e * inv);
+    H[5] = static_cast<float>((dd + e + 2.0 * y0) * inv);
+    H[6] = static_cast<float>(g * inv);
+    H[7] = static_cast<float>(h * inv);
+    H[8] = static_cast<float>(w * inv);
+}
 
 // ===========================================================================
 // 9. Finalize one (frame, family): detections in candidate order (first
@@ -28,8 +62,6 @@ __device__ __forceinline__ void stage_finalize(const BatchDesc* __restrict__ b, 
                                                FinalSmem& sm) {
     DecodeOut* s_in = sm.in;
     DecodeOut* s_out = sm.out;
-    int* s_in_src = sm.in_src;
-    int* s_out_src = sm.out_src;
     float* s_cx = sm.cx;
     float* s_cy = sm.cy;
     uint32_t* s_warp = sm.warp;
@@ -61,7 +93,6 @@ __device__ __forceinline__ void stage_finalize(const BatchDesc* __restrict__ b, 
         const int pos = before + __popc(bal & lanemask_lt());
         if (ok && pos < maxd) {
             s_in[pos] = dec[i];
-            s_in_src[pos] = i;
         }
         __syncthreads();
         if (tid == 0) {
@@ -103,13 +134,11 @@ __device__ __forceinline__ void stage_finalize(const BatchDesc* __restrict__ b, 
                 if (duplicate >= 0) {
                     if (dd.margin > s_out[duplicate].margin) {
                         s_out[duplicate] = dd;
-                        s_out_src[duplicate] = s_in_src[i];
                         s_cx[duplicate] = cx;
                         s_cy[duplicate] = cy;
                     }
                 } else if (kept < maxd) {
                     s_out[kept] = dd;
-                    s_out_src[kept] = s_in_src[i];
                     s_cx[kept] = cx;
                     s_cy[kept] = cy;
                 }
@@ -135,8 +164,7 @@ __device__ __forceinline__ void stage_finalize(const BatchDesc* __restrict__ b, 
         r.decision_margin = s_out[i].margin;
         for (int k = 0; k < 8; ++k) r.corners[k] = s_out[i].corners[k];
         r.reserved = 0;
-        const float* hsrc = d.dec_h + (static_cast<int64_t>(fam) * d.max_candidates + s_out_src[i]) * 9;
-        for (int k = 0; k < 9; ++k) r.homography[k] = hsrc[k];
+        fill_homography(r.corners, r.homography);
         dets[rank] = r;
     }
     if (tid == 0) hdr->found[fam] = static_cast<uint32_t>(kept);

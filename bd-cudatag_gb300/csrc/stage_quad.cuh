@@ -1,6 +1,6 @@
 // Quad fit and decode of the candidates as device functions: hull, four
-// corners, edge refinement, the four rotations of each quad, FP64
-// homography; one (small candidate, family) item per warp (fit_small_item)
+// corners, edge refinement, the four rotations of each quad; one (small
+// candidate, family) item per warp (fit_small_item)
 // or one big candidate per CTA (fit_big_item).  The per-stage kernels
 // (k_quad.cu) and the persistent kernel (k_persistent.cu) both call them.  All FP32
 // arithmetic follows the reference expressions term by term and is compiled
@@ -18,41 +18,6 @@ namespace {
 
 __device__ const uint64_t d_codes36h11[BD_CODEWORDS_36H11_COUNT] = {BD_CODEWORDS_36H11};
 __device__ const uint64_t d_codes16h5[BD_CODEWORDS_16H5_COUNT] = {BD_CODEWORDS_16H5};
-
-// Image homography of a decoded tag's corners (reference host
-// fill_homography :1739-1774, FP64 as there).  Computed by the warp that
-// decodes the candidate, so k_finalize only copies it.
-__device__ void fill_homography(const float corners[8], float H[9]) {
-    const double x0 = corners[0], y0 = corners[1];
-    const double x1 = corners[2], y1 = corners[3];
-    const double x2 = corners[4], y2 = corners[5];
-    const double x3 = corners[6], y3 = corners[7];
-    const double dx1 = x1 - x2, dx2 = x3 - x2;
-    const double dx3 = x0 - x1 + x2 - x3;
-    const double dy1 = y1 - y2, dy2 = y3 - y2;
-    const double dy3 = y0 - y1 + y2 - y3;
-    double g = 0.0, h = 0.0;
-    const double det = dx1 * dy2 - dx2 * dy1;
-    if (fabs(det) > 1e-12) {
-        g = (dx3 * dy2 - dx2 * dy3) / det;
-        h = (dx1 * dy3 - dx3 * dy1) / det;
-    }
-    const double a = x1 - x0 + g * x1;
-    const double bb = x3 - x0 + h * x3;
-    const double dd = y1 - y0 + g * y1;
-    const double e = y3 - y0 + h * y3;
-    const double w = g + h + 2.0;
-    const double inv = (fabs(w) > 1e-12) ? 1.0 / w : 0.0;
-    H[0] = static_cast<float>(a * inv);
-    H[1] = static_cast<float>(bb * inv);
-    H[2] = static_cast<float>((a + bb + 2.0 * x0) * inv);
-    H[3] = static_cast<float>(dd * inv);
-    H[4] = static_cast<float>(e * inv);
-    H[5] = static_cast<float>((dd + e + 2.0 * y0) * inv);
-    H[6] = static_cast<float>(g * inv);
-    H[7] = static_cast<float>(h * inv);
-    H[8] = static_cast<float>(w * inv);
-}
 
 // ===========================================================================
 // 7. Quad fit (reference k_fit_quads :1081-1241 and helpers :659-1076).
@@ -912,10 +877,6 @@ __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uin
                 out->hamming = sm.res.hamming;
                 out->margin = sm.res.margin;
                 for (int k = 0; k < 8; ++k) out->corners[k] = sm.res.corners[k];
-                float hm[9];
-                fill_homography(sm.res.corners, hm);
-                float* hout = d.dec_h + (static_cast<int64_t>(fam) * mc + ci) * 9;
-                for (int k = 0; k < 9; ++k) hout[k] = hm[k];
             }
         }
         __syncwarp();
@@ -1202,10 +1163,6 @@ __device__ __forceinline__ void fit_big_item(const BatchDesc* __restrict__ b,
             out->hamming = sm.s_res[pick].hamming;
             out->margin = sm.s_res[pick].margin;
             for (int k = 0; k < 8; ++k) out->corners[k] = sm.s_res[pick].corners[k];
-            float hm[9];
-            fill_homography(sm.s_res[pick].corners, hm);
-            float* hout = d.dec_h + (static_cast<int64_t>(fam_of_slot[tid]) * mc + ci) * 9;
-            for (int k = 0; k < 9; ++k) hout[k] = hm[k];
         }
     }
     __syncthreads();
