@@ -13,11 +13,13 @@ struct FinalSmem {
     DecodeOut in[kMaxDetectionsCap];
     DecodeOut out[kMaxDetectionsCap];
     float cx[kMaxDetectionsCap], cy[kMaxDetectionsCap];
+    float h[kMaxDetectionsCap][9];     // homography of each compacted detection
+    int out_in[kMaxDetectionsCap];     // compacted index of each kept detection
     uint32_t warp[kFinalThreads / 32];
     int count, kept;
 };
 
-// Image homography of a final detection's corners (reference host
+// Image homography of a detection's corners (reference host
 // fill_homography :1739-1774, FP64 as there), one detection per thread of
 // the finalizing CTA.
 __device__ void fill_homography(const float corners[8], float H[9]) {
@@ -104,8 +106,12 @@ __device__ __forceinline__ void stage_finalize(const BatchDesc* __restrict__ b, 
         if (sm.count >= maxd) break;
     }
     const int m = min(sm.count, maxd);
-    // De-duplication in arrival order, one warp.
-    if (warp == 0) {
+    // De-duplication in arrival order, one warp; the other warps meanwhile
+    // form the homography of every compacted detection (FP64 is slow, and
+    // the kept ones are among them).
+    if (warp > 0) {
+        for (int i = tid - 32; i < m; i += kFinalThreads - 32) fill_homography(s_in[i].corners, sm.h[i]);
+    } else {
         int kept = 0;
         for (int i = 0; i < m; ++i) {
             const DecodeOut& dd = s_in[i];
@@ -134,11 +140,13 @@ __device__ __forceinline__ void stage_finalize(const BatchDesc* __restrict__ b, 
                 if (duplicate >= 0) {
                     if (dd.margin > s_out[duplicate].margin) {
                         s_out[duplicate] = dd;
+                        sm.out_in[duplicate] = i;
                         s_cx[duplicate] = cx;
                         s_cy[duplicate] = cy;
                     }
                 } else if (kept < maxd) {
                     s_out[kept] = dd;
+                    sm.out_in[kept] = i;
                     s_cx[kept] = cx;
                     s_cy[kept] = cy;
                 }
@@ -164,7 +172,7 @@ __device__ __forceinline__ void stage_finalize(const BatchDesc* __restrict__ b, 
         r.decision_margin = s_out[i].margin;
         for (int k = 0; k < 8; ++k) r.corners[k] = s_out[i].corners[k];
         r.reserved = 0;
-        fill_homography(r.corners, r.homography);
+        for (int k = 0; k < 9; ++k) r.homography[k] = sm.h[sm.out_in[i]][k];
         dets[rank] = r;
     }
     if (tid == 0) hdr->found[fam] = static_cast<uint32_t>(kept);
