@@ -257,7 +257,8 @@ def read_traffic():
 
 
 def measure_roofline(plan, frame_sets, peaks, frames_per_s):
-    """The pipeline's roofline figure and per-stage CUDA-event times.
+    """The pipeline's roofline figure, per-stage CUDA-event times and the
+    GPU time of one batch as a graph replay.
 
     Pipeline: the algorithmic bytes are W*H per frame (the frame read once),
     so achieved = frames/s * W*H over the timed wall of the batched loop.
@@ -276,6 +277,13 @@ def measure_roofline(plan, frame_sets, peaks, frames_per_s):
         n += 1
     mean = {s: v / n for s, v in sums.items()}
     total = sum(mean.values())
+    # One batch as the graph runs it (the two fit kernels side by side):
+    # median GPU time of 50 replays after 10, CUDA events around the launch.
+    single = []
+    for k in range(60):
+        plan.detect(frame_sets[k % len(frame_sets)], [W] * BATCH, device=True)
+        if k >= 10:
+            single.append(plan.last_gpu_ms())
     T = ((W + 7) // 8) * ((H + 7) // 8)
     per_frame = {
         "stats": W * H + 2 * T,                              # frame read once, tile min/max written
@@ -306,6 +314,8 @@ def measure_roofline(plan, frame_sets, peaks, frames_per_s):
         "kernels": kernels,
         "stage_ms": {k: round(v, 5) for k, v in mean.items()},
         "stage_ms_sum": round(total, 5),
+        "stage_ms_note": "un-graphed, one kernel after another (the fit kernels too)",
+        "single_batch_gpu_ms": round(float(np.median(single)), 5),
         "stage_share": {k: round(v / total, 4) for k, v in mean.items()},
         "latency_bound": "stages other than stats and binarize_runs: L2 gathers and union-find "
                          "walks, reported as time",
