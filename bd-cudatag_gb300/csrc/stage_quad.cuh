@@ -171,9 +171,8 @@ __device__ __forceinline__ bool intersect_lines(const float li[4], const float l
 
 // Bilinear sample with the reference's bounds rule (sample_bilinear
 // :833-849): -1 outside [0, width-1) x [0, height-1).  The address is
-// clamped and the result selected instead of branching, so the loads of
-// consecutive probes can be in flight together; in-range values are computed
-// with the reference's expression.
+// clamped and the result selected instead of branching; in-range values are
+// computed with the reference's expression.
 __device__ __forceinline__ float sample_ro(const uint8_t* __restrict__ image, int width, int height,
                                            int64_t stride, float x, float y) {
     const bool in = x >= 0.0f && y >= 0.0f && x < static_cast<float>(width - 1) &&
@@ -256,25 +255,18 @@ __device__ void fit_edges_warp(const float (*q)[2], const uint8_t* __restrict__ 
                 const float py = ay + alpha * ey;
                 float best_mag = 0.0f;
                 int best = -1;
-                // Four independent rises per block (indices past the end
-                // repeat the last probe and are dropped), then the
-                // reference's in-order peak scan over the block.
-                for (int i0 = 0; i0 < probes; i0 += 4) {
-                    float m[4];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const int i = min(i0 + j, probes - 1);
-                        const float t = step * static_cast<float>(i - half);
-                        m[j] = rise_ro(image, width, height, stride, px + nx * t, py + ny * t, nx, ny);
-                    }
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        if (i0 + j >= probes) break;
-                        mags[i0 + j] = m[j];
-                        if (m[j] > best_mag) {
-                            best_mag = m[j];
-                            best = i0 + j;
-                        }
+                // One rise per probe, in order, with the reference's peak
+                // scan.  (Blocks of four probes, the last block padded with
+                // repeats of the last probe, issued more instructions for
+                // the same result: the fit kernels are bound by the
+                // instructions their warps issue, not by load latency.)
+                for (int i = 0; i < probes; ++i) {
+                    const float t = step * static_cast<float>(i - half);
+                    const float m = rise_ro(image, width, height, stride, px + nx * t, py + ny * t, nx, ny);
+                    mags[i] = m;
+                    if (m > best_mag) {
+                        best_mag = m;
+                        best = i;
                     }
                 }
                 if (first_pass && best > 2) {
@@ -801,17 +793,19 @@ __device__ __forceinline__ void row_extremes(const FrameDesc& d, uint32_t root, 
         }
     }
     int left = -1, right = -1;
-    for (int k = first; k < n; k += 4) {
-        uint32_t rr[4], lab[4];
+    // Runs two at a time (no padding loads past the end of the row).
+    for (int k = first; k < n; k += 2) {
+        uint32_t rr[2] = {}, lab[2] = {};
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int kk = min(k + j, n - 1);
-            rr[j] = row_runs[kk];
-            lab[j] = row_label[kk];
+        for (int j = 0; j < 2; ++j) {
+            if (k + j < n) {
+                rr[j] = row_runs[k + j];
+                lab[j] = row_label[k + j];
+            }
         }
         bool stop = false;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < 2; ++j) {
             if (stop || k + j >= n) continue;
             const int rx0 = static_cast<int>(rr[j] & 0xffffu);
             const int rx1 = static_cast<int>(rr[j] >> 16);
@@ -910,9 +904,13 @@ __device__ __forceinline__ void fit_small_item(const BatchDesc* __restrict__ b,
 
     // Boundary points in reference order (row s: left, then right) go
     // to every lane by shuffles; lane = direction keeps the first point
-    // of largest projection.
+    // of largest projection.  The points travel as float coordinates,
+    // converted once by the lane that found them (NaN for a row without a
+    // point: its projection never wins), and the winning point's packed
+    // form is fetched once per round.
     float best_dot = -FLT_MAX;
     uint32_t best_point = kNone;
+    const float none = bdmath::quiet_nan();
     for (int s0 = 0; s0 < kept; s0 += 32) {
         uint32_t lp = kNone, rp = kNone;
         const int s = s0 + lane;
@@ -920,27 +918,29 @@ __device__ __forceinline__ void fit_small_item(const BatchDesc* __restrict__ b,
             const int y = y0 + (kept == rows ? s : (s * (rows - 1)) / (kept - 1));  // kept < rows: kept > 1
             row_extremes(d, root, x0, x1, y, &lp, &rp);
         }
+        const float lx = lp != kNone ? static_cast<float>(lp & 0xffffu) : none;
+        const float ly = lp != kNone ? static_cast<float>(lp >> 16) : none;
+        const float rx = rp != kNone ? static_cast<float>(rp & 0xffffu) : none;
+        const float ry = rp != kNone ? static_cast<float>(rp >> 16) : none;
         const int count = min(32, kept - s0);
+        int pick = -1;  // 2 * row + side of this round's best point
         for (int k = 0; k < count; ++k) {
-            const uint32_t pl = __shfl_sync(kFull, lp, k);
-            const uint32_t pr = __shfl_sync(kFull, rp, k);
-            if (pl != kNone) {
-                const float dd =
-                    static_cast<float>(pl & 0xffffu) * ux + static_cast<float>(pl >> 16) * uy;
-                if (dd > best_dot) {
-                    best_dot = dd;
-                    best_point = pl;
-                }
+            const float ax = __shfl_sync(kFull, lx, k), ay = __shfl_sync(kFull, ly, k);
+            const float bx = __shfl_sync(kFull, rx, k), by = __shfl_sync(kFull, ry, k);
+            const float dl = ax * ux + ay * uy;
+            if (dl > best_dot) {
+                best_dot = dl;
+                pick = 2 * k;
             }
-            if (pr != kNone) {
-                const float dd =
-                    static_cast<float>(pr & 0xffffu) * ux + static_cast<float>(pr >> 16) * uy;
-                if (dd > best_dot) {
-                    best_dot = dd;
-                    best_point = pr;
-                }
+            const float dr = bx * ux + by * uy;
+            if (dr > best_dot) {
+                best_dot = dr;
+                pick = 2 * k + 1;
             }
         }
+        const uint32_t cl = __shfl_sync(kFull, lp, max(pick, 0) >> 1);
+        const uint32_t cr = __shfl_sync(kFull, rp, max(pick, 0) >> 1);
+        if (pick >= 0) best_point = (pick & 1) ? cr : cl;
     }
     // Hull: extremes in direction order without repeats of the previous
     // kept point, and without a last point equal to the first.  The
