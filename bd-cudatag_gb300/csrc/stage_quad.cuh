@@ -433,7 +433,7 @@ __device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8
         px = ax + alpha * ex;
         py = ay + alpha * ey;
         float* mags = s_mags + sample * kMaxProbes;
-#pragma unroll 8
+#pragma unroll 1
         for (int i = parity; i < probes; i += 2) {
             const float t = step * static_cast<float>(i - half);
             mags[i] = rise_ro(image, width, height, stride, px + nx * t, py + ny * t, nx, ny);
