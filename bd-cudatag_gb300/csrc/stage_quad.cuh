@@ -257,9 +257,8 @@ __device__ void fit_edges_warp(const float (*q)[2], const uint8_t* __restrict__ 
                 int best = -1;
                 // One rise per probe, in order, with the reference's peak
                 // scan.  (Blocks of four probes, the last block padded with
-                // repeats of the last probe, issued more instructions for
-                // the same result: the fit kernels are bound by the
-                // instructions their warps issue, not by load latency.)
+                // repeats of the last probe to keep loads in flight, issued
+                // more instructions for the same result and ran slower.)
                 for (int i = 0; i < probes; ++i) {
                     const float t = step * static_cast<float>(i - half);
                     const float m = rise_ro(image, width, height, stride, px + nx * t, py + ny * t, nx, ny);
