@@ -269,16 +269,21 @@ __device__ void fit_edges_warp(const float (*q)[2], const uint8_t* __restrict__ 
                     }
                 }
                 if (first_pass && best > 2) {
+                    // The reference takes the first i in [1, best - 2] that is a local
+                    // peak of at least 0.70 * best_mag with min(mags[i + 1 .. best - 1])
+                    // below half of it.  One pass from the right with a running minimum
+                    // finds the same i (the last one recorded) without the inner loop.
                     const float accept = 0.70f * best_mag;
-                    for (int i = 1; i + 1 < best; ++i) {
+                    float valley = FLT_MAX;
+                    int first = -1;
+                    for (int i = best - 2; i >= 1; --i) {
+                        valley = fminf(valley, mags[i + 1]);
                         if (mags[i] < accept || mags[i] < mags[i - 1] || mags[i] < mags[i + 1]) continue;
-                        float valley = FLT_MAX;
-                        for (int k = i + 1; k < best; ++k) valley = fminf(valley, mags[k]);
-                        if (valley < 0.5f * mags[i]) {
-                            best = i;
-                            best_mag = mags[i];
-                            break;
-                        }
+                        if (valley < 0.5f * mags[i]) first = i;
+                    }
+                    if (first >= 0) {
+                        best = first;
+                        best_mag = mags[first];
                     }
                 }
                 if (best >= 0 && best_mag >= 6.0f) {
@@ -454,16 +459,21 @@ __device__ bool fit_edge_line_warp(const float quad[4][2], int edge, const uint8
             }
         }
         if (first_pass && best > 2) {
+            // The reference takes the first i in [1, best - 2] that is a local
+            // peak of at least 0.70 * best_mag with min(mags[i + 1 .. best - 1])
+            // below half of it.  One pass from the right with a running minimum
+            // finds the same i (the last one recorded) without the inner loop.
             const float accept = 0.70f * best_mag;
-            for (int i = 1; i + 1 < best; ++i) {
+            float valley = FLT_MAX;
+            int first = -1;
+            for (int i = best - 2; i >= 1; --i) {
+                valley = fminf(valley, mags[i + 1]);
                 if (mags[i] < accept || mags[i] < mags[i - 1] || mags[i] < mags[i + 1]) continue;
-                float valley = FLT_MAX;
-                for (int k = i + 1; k < best; ++k) valley = fminf(valley, mags[k]);
-                if (valley < 0.5f * mags[i]) {
-                    best = i;
-                    best_mag = mags[i];
-                    break;
-                }
+                if (valley < 0.5f * mags[i]) first = i;
+            }
+            if (first >= 0) {
+                best = first;
+                best_mag = mags[first];
             }
         }
         if (best >= 0 && best_mag >= 6.0f) {
