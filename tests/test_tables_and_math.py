@@ -95,3 +95,58 @@ def test_otsu_prefix_exact_below_2_24():
             s = np.float32(s + np.float32(i) * np.float32(hist[i]))
             assert total == np.float32(np.sum(hist[:i + 1]))
             assert s == np.float32(np.dot(np.arange(i + 1), hist[:i + 1]))
+
+
+def _valley_reference(mags, best, best_mag):
+    """The reference's first-pass test (gpu_detector.cu fit_edge_line_warp):
+    the first i in [1, best - 2] that is a local peak of at least 0.70 *
+    best_mag with min(mags[i + 1 .. best - 1]) below half of it."""
+    accept = np.float32(0.70) * best_mag
+    for i in range(1, best - 1):
+        if mags[i] < accept or mags[i] < mags[i - 1] or mags[i] < mags[i + 1]:
+            continue
+        valley = np.float32(np.finfo(np.float32).max)
+        for k in range(i + 1, best):
+            valley = min(valley, mags[k])
+        if valley < np.float32(0.5) * mags[i]:
+            return i, mags[i]
+    return best, best_mag
+
+
+def _valley_one_pass(mags, best, best_mag):
+    """The kernels' form (stage_quad.cuh, fit_edges_warp and
+    fit_edge_line_warp): one pass from the right with a running minimum; the
+    last index recorded is the first qualifying one."""
+    accept = np.float32(0.70) * best_mag
+    valley = np.float32(np.finfo(np.float32).max)
+    first = -1
+    for i in range(best - 2, 0, -1):
+        valley = min(valley, mags[i + 1])
+        if mags[i] < accept or mags[i] < mags[i - 1] or mags[i] < mags[i + 1]:
+            continue
+        if valley < np.float32(0.5) * mags[i]:
+            first = i
+    return (first, mags[first]) if first >= 0 else (best, best_mag)
+
+
+def test_valley_one_pass_matches_reference_loop():
+    """The one-pass valley test picks the same probe as the reference's
+    quadratic loop, on random rise profiles with ties, plateaus and zeros."""
+    rng = np.random.default_rng(5)
+    for trial in range(4000):
+        probes = int(rng.integers(5, 50))
+        kind = trial % 3
+        if kind == 0:
+            mags = rng.uniform(0, 60, probes)
+        elif kind == 1:
+            mags = rng.integers(0, 6, probes) * 10.0  # many ties
+        else:
+            mags = np.abs(np.sin(np.arange(probes) * rng.uniform(0.2, 1.5))) * rng.uniform(5, 80)
+        mags = mags.astype(np.float32)
+        best, best_mag = -1, np.float32(0.0)
+        for i, m in enumerate(mags):  # in-order peak scan, strict >
+            if m > best_mag:
+                best, best_mag = i, m
+        if best <= 2:
+            continue
+        assert _valley_one_pass(mags, best, best_mag) == _valley_reference(mags, best, best_mag)
