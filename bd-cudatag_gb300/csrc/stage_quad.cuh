@@ -859,18 +859,20 @@ __device__ void fit_decode_family(const FrameDesc& d, int fam, int ci, const uin
 
         // Decode: the refined quad's rotations, then the hull quad's only
         // when none of those decoded and refinement moved a corner (an
-        // unmoved quad would decode the same way again).
-        int best = decode_rotations_warp(gray, d, stride, fam, &sm.q[0][0], lane, cell_uv, sm.cells.raw,
-                                         sm.cells.sharp, &sm.res);
+        // unmoved quad would decode the same way again).  One call site in
+        // a loop that is not unrolled keeps one copy of the decode code.
         bool moved = false;
         {
             const float* qa = &sm.q[0][0];
             const float* qb = &sm.hq[0][0];
             for (int k = 0; k < 8; ++k) moved = moved || __float_as_uint(qa[k]) != __float_as_uint(qb[k]);
         }
-        if (best < 0 && moved) {
-            best = decode_rotations_warp(gray, d, stride, fam, &sm.hq[0][0], lane, cell_uv, sm.cells.raw,
-                                         sm.cells.sharp, &sm.res);
+        int best = -1;
+#pragma unroll 1
+        for (int variant = 0; variant < 2; ++variant) {
+            if (variant == 1 && (best >= 0 || !moved)) break;
+            best = decode_rotations_warp(gray, d, stride, fam, variant == 0 ? &sm.q[0][0] : &sm.hq[0][0], lane,
+                                         cell_uv, sm.cells.raw, sm.cells.sharp, &sm.res);
         }
         if (lane == 0) {
             if (best < 0) {
