@@ -140,24 +140,6 @@ __device__ bool hull_to_quad_warp(const uint32_t* hull, int count, float quad[4]
     return ok != 0;
 }
 
-__device__ __forceinline__ float sample_bilinear(const uint8_t* image, int width, int height,
-                                                 int64_t stride, float x, float y) {
-    if (!(x >= 0.0f && y >= 0.0f && x < static_cast<float>(width - 1) &&
-          y < static_cast<float>(height - 1))) {
-        return -1.0f;
-    }
-    const int ix = static_cast<int>(x);
-    const int iy = static_cast<int>(y);
-    const float fx = x - static_cast<float>(ix);
-    const float fy = y - static_cast<float>(iy);
-    const uint8_t* p = image + static_cast<int64_t>(iy) * stride + ix;
-    const float a = p[0];
-    const float bb = p[1];
-    const float c = p[stride];
-    const float dd = p[stride + 1];
-    return (a * (1.0f - fx) + bb * fx) * (1.0f - fy) + (c * (1.0f - fx) + dd * fx) * fy;
-}
-
 __device__ __forceinline__ bool intersect_lines(const float li[4], const float lj[4], float* x,
                                                 float* y) {
     const float det = li[2] * lj[3] - li[3] * lj[2];
@@ -603,7 +585,7 @@ __device__ int decode_rotations_warp(const uint8_t* __restrict__ gray, const Fra
             }
             const float x = (h[0] * uu + h[1] * vv + h[2]) / den;
             const float y = (h[3] * uu + h[4] * vv + h[5]) / den;
-            const float value = sample_bilinear(gray, d.width, d.height, stride, x - 0.0f, y - 0.0f);
+            const float value = sample_ro(gray, d.width, d.height, stride, x - 0.0f, y - 0.0f);
             if (value < 0.0f) valid = false;
             raw[c] = value;
             mn = fminf(mn, value);
